@@ -1,0 +1,575 @@
+// C ABI of the hydro step: argument checking, the task entry points, the solver
+// object (work buffers + the time loop of apps/hydro/driver.h:317-413) and the
+// device-memory helpers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "flecsale_gb300.h"
+#include "fvh_internal.h"
+#include "fvh_kernels.h"
+#include "fvh_mixed.h"
+
+namespace {
+
+inline cudaStream_t cs(fvh_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline fvh_status from_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return FVH_OK;
+  if (e == cudaErrorMemoryAllocation) return FVH_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FVH_ERR_NO_DEVICE;
+  return FVH_ERR_CUDA;
+}
+
+bool mesh_ok(const fvh_mesh_view *m) {
+  if (!m || (m->dim != 2 && m->dim != 3) || m->num_cells <= 0 || m->num_faces <= 0)
+    return false;
+  if (!m->face_cells || !m->cell_face_offsets || !m->cell_faces || !m->cell_nbr_offsets ||
+      !m->cell_nbrs || !m->cell_vertex_offsets || !m->cell_vertices || !m->cell_volume ||
+      !m->face_area)
+    return false;
+  for (int d = 0; d < m->dim; ++d)
+    if (!m->cell_centroid[d] || !m->face_centroid[d] || !m->face_normal[d] ||
+        !m->vertex_coord[d])
+      return false;
+  return true;
+}
+
+bool state_ok(const fvh_state_view *s, int dim) {
+  if (!s || !s->density || !s->internal_energy || !s->pressure || !s->temperature ||
+      !s->sound_speed)
+    return false;
+  for (int d = 0; d < dim; ++d)
+    if (!s->velocity[d]) return false;
+  return true;
+}
+
+bool grads_ok(const fvh_gradient_view *g, int dim) {
+  if (!g) return false;
+  for (int i = 0; i < dim; ++i) {
+    if (!g->density[i] || !g->internal_energy[i] || !g->pressure[i] || !g->sound_speed[i])
+      return false;
+    for (int d = 0; d < dim; ++d)
+      if (!g->velocity[d][i]) return false;
+  }
+  return true;
+}
+
+bool flux_ok(const fvh_flux_view *f, int dim) {
+  if (!f || !f->mass || !f->energy) return false;
+  for (int d = 0; d < dim; ++d)
+    if (!f->momentum[d]) return false;
+  return true;
+}
+
+bool params_ok(const fvh_params *p, int dim) {
+  return p && p->dim == dim && p->flux_kind >= 0 && p->flux_kind <= 2 &&
+         p->limiter >= 0 && p->limiter <= 1 && (p->order == 1 || p->order == 2) &&
+         (p->precision == FVH_PRECISION_FP64 || p->precision == FVH_PRECISION_MIXED) &&
+         p->gamma > 1 && p->cv > 0 && p->cfl > 0;
+}
+
+int dt_blocks(int num_cells) {
+  int nb = (num_cells + fvh::kDtThreads - 1) / fvh::kDtThreads;
+  return nb < fvh::kDtMaxBlocks ? nb : fvh::kDtMaxBlocks;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// solver object
+// ---------------------------------------------------------------------------
+struct fvh_solver {
+  fvh_mesh_view mesh{};
+  fvh_params params{};
+  fvh_gradient_view grads{};
+  fvh_flux_view flux{};
+  double *work = nullptr;          // gradients + fluxes
+  double *scalars = nullptr;       // [0] soln time, [1] dt, [2..] dt partials
+  fvh_device_status *status = nullptr;
+  double *host_scalars = nullptr;  // pinned: soln time
+  fvh_device_status *host_status = nullptr;
+  fvh::mixed::workspace *mixed = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  fvh_state_view graph_state{};
+};
+
+struct fvh_device_mesh {
+  fvh_mesh_view view{};
+  std::vector<void *> allocs;
+};
+
+struct fvh_device_state {
+  fvh_state_view view{};
+  double *base = nullptr;
+};
+
+extern "C" {
+
+const char *fvh_status_string(int32_t s) {
+  switch (s) {
+    case FVH_OK: return "ok";
+    case FVH_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case FVH_ERR_CUDA: return "CUDA runtime error";
+    case FVH_ERR_INFINITE_DT: return "infinite delta t";
+    case FVH_ERR_NEGATIVE_STATE: return "Negative density or internal energy encountered!";
+    case FVH_ERR_UNSUPPORTED: return "unsupported mesh or option";
+    case FVH_ERR_NO_DEVICE: return "no CUDA device";
+    case FVH_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case FVH_ERR_CAPACITY: return "request exceeds a fixed capacity";
+    default: return "unknown status";
+  }
+}
+
+int32_t fvh_abi_version(void) { return FVH_ABI_VERSION; }
+
+void fvh_params_default(fvh_params *p, int32_t dim) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->dim = dim;
+  p->flux_kind = FVH_FLUX_HLLE;
+  p->limiter = FVH_LIMITER_BARTH_JESPERSEN;
+  p->order = 2;
+  p->recon_swap_ep = 1;
+  p->precision = FVH_PRECISION_FP64;
+  p->gamma = 1.4;
+  p->cv = 1.0;
+  p->cfl = dim == 3 ? 1.0 / 3.0 : 0.5;
+  p->final_time = 0.2;
+}
+
+void fvh_status_decode(fvh_device_status s, int32_t *code, int64_t *cell) {
+  if (s == FVH_STATUS_CLEAR) {
+    if (code) *code = FVH_OK;
+    if (cell) *cell = -1;
+    return;
+  }
+  if (code) *code = (int32_t)(s & 0xff);
+  if (cell) *cell = (int64_t)(s >> 8);
+}
+
+size_t fvh_time_step_workspace_bytes(int32_t num_cells) {
+  return sizeof(double) * (size_t)dt_blocks(num_cells > 0 ? num_cells : 1);
+}
+
+fvh_status fvh_evaluate_time_step(const fvh_mesh_view *mesh, const fvh_state_view *state,
+                                  const fvh_params *params, const double *d_soln_time,
+                                  double *d_dt, void *d_workspace, size_t workspace_bytes,
+                                  fvh_device_status *d_status, fvh_stream_t stream) {
+  if (!mesh_ok(mesh) || !state_ok(state, mesh->dim) || !params_ok(params, mesh->dim) ||
+      !d_soln_time || !d_dt || !d_workspace || !d_status ||
+      workspace_bytes < fvh_time_step_workspace_bytes(mesh->num_cells))
+    return FVH_ERR_INVALID_ARGUMENT;
+  const int nb = dt_blocks(mesh->num_cells);
+  double *partial = static_cast<double *>(d_workspace);
+  const cudaError_t e =
+      mesh->dim == 2
+          ? fvh::plain::launch_dt<2>(*mesh, *state, *params, d_soln_time, d_dt, partial, nb,
+                                     d_status, cs(stream))
+          : fvh::plain::launch_dt<3>(*mesh, *state, *params, d_soln_time, d_dt, partial, nb,
+                                     d_status, cs(stream));
+  return from_cuda(e);
+}
+
+fvh_status fvh_evaluate_gradients(const fvh_mesh_view *mesh, const fvh_state_view *state,
+                                  const fvh_gradient_view *grads, const fvh_params *params,
+                                  fvh_stream_t stream) {
+  if (!mesh_ok(mesh) || !state_ok(state, mesh->dim) || !grads_ok(grads, mesh->dim) ||
+      !params_ok(params, mesh->dim))
+    return FVH_ERR_INVALID_ARGUMENT;
+  if (params->order == 1) {
+    // first order: zero gradients
+    const int D = mesh->dim;
+    for (int i = 0; i < D; ++i) {
+      const size_t b = sizeof(double) * mesh->num_cells;
+      cudaMemsetAsync(grads->density[i], 0, b, cs(stream));
+      cudaMemsetAsync(grads->internal_energy[i], 0, b, cs(stream));
+      cudaMemsetAsync(grads->pressure[i], 0, b, cs(stream));
+      cudaMemsetAsync(grads->sound_speed[i], 0, b, cs(stream));
+      for (int d = 0; d < D; ++d) cudaMemsetAsync(grads->velocity[d][i], 0, b, cs(stream));
+    }
+    return from_cuda(cudaGetLastError());
+  }
+  const cudaError_t e =
+      mesh->dim == 2 ? fvh::plain::launch_gradients<2>(*mesh, *state, *grads, *params, cs(stream))
+                     : fvh::plain::launch_gradients<3>(*mesh, *state, *grads, *params, cs(stream));
+  return from_cuda(e);
+}
+
+fvh_status fvh_evaluate_fluxes(const fvh_mesh_view *mesh, const fvh_state_view *state,
+                               const fvh_gradient_view *grads, const fvh_flux_view *flux,
+                               const fvh_params *params, fvh_stream_t stream) {
+  if (!mesh_ok(mesh) || !state_ok(state, mesh->dim) || !grads_ok(grads, mesh->dim) ||
+      !flux_ok(flux, mesh->dim) || !params_ok(params, mesh->dim))
+    return FVH_ERR_INVALID_ARGUMENT;
+  const cudaError_t e =
+      mesh->dim == 2
+          ? fvh::plain::launch_fluxes<2>(*mesh, *state, *grads, *flux, *params, cs(stream))
+          : fvh::plain::launch_fluxes<3>(*mesh, *state, *grads, *flux, *params, cs(stream));
+  return from_cuda(e);
+}
+
+fvh_status fvh_apply_update(const fvh_mesh_view *mesh, const fvh_params *params,
+                            const double *d_dt, double factor, const fvh_flux_view *flux,
+                            const fvh_state_view *state, double *d_soln_time,
+                            fvh_device_status *d_status, fvh_stream_t stream) {
+  if (!mesh_ok(mesh) || !state_ok(state, mesh->dim) || !flux_ok(flux, mesh->dim) ||
+      !params_ok(params, mesh->dim) || !d_dt || !d_soln_time || !d_status)
+    return FVH_ERR_INVALID_ARGUMENT;
+  const cudaError_t e =
+      mesh->dim == 2 ? fvh::plain::launch_update<2>(*mesh, *params, d_dt, factor, *flux, *state,
+                                                    d_soln_time, d_status, cs(stream))
+                     : fvh::plain::launch_update<3>(*mesh, *params, d_dt, factor, *flux, *state,
+                                                    d_soln_time, d_status, cs(stream));
+  return from_cuda(e);
+}
+
+// ---------------------------------------------------------------------------
+// solver
+// ---------------------------------------------------------------------------
+void fvh_solver_destroy(fvh_solver *s) {
+  if (!s) return;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->mixed) fvh::mixed::destroy(s->mixed);
+  cudaFree(s->work);
+  cudaFree(s->scalars);
+  cudaFree(s->status);
+  cudaFreeHost(s->host_scalars);
+  cudaFreeHost(s->host_status);
+  delete s;
+}
+
+fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params,
+                             fvh_solver **out) {
+  if (!out || !mesh_ok(mesh) || !params_ok(params, mesh->dim)) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  fvh_solver *s = new (std::nothrow) fvh_solver();
+  if (!s) return FVH_ERR_OUT_OF_MEMORY;
+  s->mesh = *mesh;
+  s->params = *params;
+  const int D = mesh->dim;
+  const size_t nc = mesh->num_cells, nf = mesh->num_faces;
+  const size_t ng = (size_t)(D + 4) * D;
+  cudaError_t e = cudaSuccess;
+  if (params->precision == FVH_PRECISION_FP64) {
+    e = cudaMalloc(&s->work, sizeof(double) * (ng * nc + (size_t)(D + 2) * nf));
+    if (e == cudaSuccess) {
+      double *b = s->work;
+      for (int i = 0; i < D; ++i, b += nc) s->grads.density[i] = b;
+      for (int d = 0; d < D; ++d)
+        for (int i = 0; i < D; ++i, b += nc) s->grads.velocity[d][i] = b;
+      for (int i = 0; i < D; ++i, b += nc) s->grads.internal_energy[i] = b;
+      for (int i = 0; i < D; ++i, b += nc) s->grads.pressure[i] = b;
+      for (int i = 0; i < D; ++i, b += nc) s->grads.sound_speed[i] = b;
+      s->flux.mass = b;
+      b += nf;
+      for (int i = 0; i < D; ++i, b += nf) s->flux.momentum[i] = b;
+      s->flux.energy = b;
+    }
+  } else {
+    const fvh_status ms = fvh::mixed::create(*mesh, *params, &s->mixed);
+    if (ms != FVH_OK) {
+      fvh_solver_destroy(s);
+      return ms;
+    }
+  }
+  if (e == cudaSuccess)
+    e = cudaMalloc(&s->scalars, sizeof(double) * 2 + fvh_time_step_workspace_bytes(mesh->num_cells));
+  if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(fvh_device_status));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->host_scalars, sizeof(double) * 2);
+  if (e == cudaSuccess) e = cudaMallocHost(&s->host_status, sizeof(fvh_device_status));
+  if (e == cudaSuccess) e = cudaMemset(s->scalars, 0, sizeof(double) * 2);
+  if (e == cudaSuccess) e = cudaMemset(s->status, 0xff, sizeof(fvh_device_status));
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    fvh_solver_destroy(s);
+    return from_cuda(e);
+  }
+  *out = s;
+  return FVH_OK;
+}
+
+static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state,
+                                      cudaStream_t st) {
+  const fvh_mesh_view &m = s->mesh;
+  const fvh_params &p = s->params;
+  double *t = s->scalars, *dt = s->scalars + 1, *partial = s->scalars + 2;
+  if (p.precision == FVH_PRECISION_MIXED)
+    return from_cuda(fvh::mixed::step(s->mixed, m, p, *state, t, dt, partial,
+                                      dt_blocks(m.num_cells), s->status, st));
+  const size_t wsb = fvh_time_step_workspace_bytes(m.num_cells);
+  fvh_status r = fvh_evaluate_time_step(&m, state, &p, t, dt, partial, wsb, s->status,
+                                        reinterpret_cast<fvh_stream_t>(st));
+  for (int stage = 0; stage < 2 && r == FVH_OK; ++stage) {
+    r = fvh_evaluate_gradients(&m, state, &s->grads, &p, reinterpret_cast<fvh_stream_t>(st));
+    if (r == FVH_OK)
+      r = fvh_evaluate_fluxes(&m, state, &s->grads, &s->flux, &p,
+                              reinterpret_cast<fvh_stream_t>(st));
+    if (r == FVH_OK)
+      r = fvh_apply_update(&m, &p, dt, 0.5, &s->flux, state, t, s->status,
+                           reinterpret_cast<fvh_stream_t>(st));
+  }
+  return r;
+}
+
+fvh_status fvh_solver_step(fvh_solver *s, const fvh_state_view *state, fvh_stream_t stream) {
+  if (!s || !state_ok(state, s->mesh.dim)) return FVH_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = cs(stream);
+  // One step is a fixed sequence of launches; it is captured once per
+  // (stream, state) into a CUDA graph and replayed.
+  if (st != nullptr) {
+    if (!s->graph || s->graph_stream != st ||
+        std::memcmp(&s->graph_state, state, sizeof(*state)) != 0) {
+      if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return from_cuda(e);
+      const fvh_status r = solver_step_enqueue(s, state, st);
+      e = cudaStreamEndCapture(st, &g);
+      if (r != FVH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+      }
+      if (e != cudaSuccess) return from_cuda(e);
+      e = cudaGraphInstantiate(&s->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        s->graph = nullptr;
+        return from_cuda(e);
+      }
+      s->graph_stream = st;
+      s->graph_state = *state;
+    }
+    return from_cuda(cudaGraphLaunch(s->graph, st));
+  }
+  return solver_step_enqueue(s, state, st);
+}
+
+fvh_status fvh_solver_check(fvh_solver *s, fvh_stream_t stream, double *soln_time,
+                            int64_t *bad_cell) {
+  if (!s) return FVH_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = cs(stream);
+  cudaMemcpyAsync(s->host_scalars, s->scalars, sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(s->host_status, s->status, sizeof(fvh_device_status), cudaMemcpyDeviceToHost,
+                  st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return from_cuda(e);
+  if (soln_time) *soln_time = s->host_scalars[0];
+  int32_t code;
+  int64_t cell;
+  fvh_status_decode(*s->host_status, &code, &cell);
+  if (bad_cell) *bad_cell = cell;
+  return (fvh_status)code;
+}
+
+fvh_status fvh_solver_reset(fvh_solver *s, double t, fvh_stream_t stream) {
+  if (!s) return FVH_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = cs(stream);
+  s->host_scalars[1] = t;
+  cudaError_t e = cudaMemcpyAsync(s->scalars, s->host_scalars + 1, sizeof(double),
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->status, 0xff, sizeof(fvh_device_status), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return from_cuda(e);
+}
+
+fvh_status fvh_solver_run(fvh_solver *s, const fvh_state_view *state, int64_t nsteps,
+                          int32_t stop_at_final_time, int32_t check_every,
+                          int64_t *steps_done, fvh_stream_t stream) {
+  if (!s || !state_ok(state, s->mesh.dim) || nsteps < 0) return FVH_ERR_INVALID_ARGUMENT;
+  if (check_every <= 0) check_every = 1;
+  int64_t n = 0;
+  fvh_status r = FVH_OK;
+  const double tf = s->params.final_time;
+  const double t_stop = tf - 1e-12 * std::fabs(tf);
+  while (n < nsteps) {
+    if (stop_at_final_time) {
+      double t = 0;
+      r = fvh_solver_check(s, stream, &t, nullptr);
+      if (r != FVH_OK || t >= t_stop) break;
+    }
+    const int64_t chunk = stop_at_final_time
+                              ? (nsteps - n < check_every ? nsteps - n : check_every)
+                              : nsteps - n;
+    for (int64_t k = 0; k < chunk && r == FVH_OK; ++k, ++n) r = fvh_solver_step(s, state, stream);
+    if (r != FVH_OK) break;
+  }
+  if (r == FVH_OK) r = fvh_solver_check(s, stream, nullptr, nullptr);
+  if (steps_done) *steps_done = n;
+  return r;
+}
+
+double *fvh_solver_soln_time(fvh_solver *s) { return s ? s->scalars : nullptr; }
+double *fvh_solver_dt(fvh_solver *s) { return s ? s->scalars + 1 : nullptr; }
+fvh_device_status *fvh_solver_status(fvh_solver *s) { return s ? s->status : nullptr; }
+const fvh_gradient_view *fvh_solver_gradients(fvh_solver *s) {
+  if (!s) return nullptr;
+  return s->params.precision == FVH_PRECISION_FP64 ? &s->grads : nullptr;
+}
+const fvh_flux_view *fvh_solver_fluxes(fvh_solver *s) {
+  if (!s) return nullptr;
+  return s->params.precision == FVH_PRECISION_FP64 ? &s->flux : nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// device memory helpers
+// ---------------------------------------------------------------------------
+void fvh_device_mesh_destroy(fvh_device_mesh *dm) {
+  if (!dm) return;
+  for (void *p : dm->allocs) cudaFree(p);
+  delete dm;
+}
+
+fvh_status fvh_device_mesh_create(const fvh_host_mesh *m, fvh_device_mesh **out) {
+  if (!m || !out) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  fvh_device_mesh *dm = new (std::nothrow) fvh_device_mesh();
+  if (!dm) return FVH_ERR_OUT_OF_MEMORY;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](const void *src, size_t bytes) -> void * {
+    if (e != cudaSuccess) return nullptr;
+    void *d = nullptr;
+    e = cudaMalloc(&d, bytes > 0 ? bytes : 16);
+    if (e != cudaSuccess) return nullptr;
+    dm->allocs.push_back(d);
+    if (bytes) e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
+    return d;
+  };
+  auto upi = [&](const std::vector<int32_t> &v) {
+    return static_cast<const int32_t *>(up(v.data(), v.size() * sizeof(int32_t)));
+  };
+  auto upd = [&](const std::vector<double> &v) {
+    return static_cast<const double *>(up(v.data(), v.size() * sizeof(double)));
+  };
+  fvh_mesh_view &o = dm->view;
+  o.dim = m->dim;
+  o.num_cells = m->nc;
+  o.num_faces = m->nf;
+  o.num_vertices = m->nv;
+  o.face_cells = upi(m->face_cells);
+  o.cell_face_offsets = upi(m->cf_off);
+  o.cell_faces = upi(m->cf);
+  o.cell_nbr_offsets = upi(m->nb_off);
+  o.cell_nbrs = upi(m->nb);
+  o.cell_vertex_offsets = upi(m->cv_off);
+  o.cell_vertices = upi(m->cv);
+  for (int d = 0; d < m->dim; ++d) {
+    o.cell_centroid[d] = upd(m->cc[d]);
+    o.face_centroid[d] = upd(m->fc[d]);
+    o.face_normal[d] = upd(m->fn[d]);
+    o.vertex_coord[d] = upd(m->vc[d]);
+  }
+  o.cell_volume = upd(m->cvol);
+  o.face_area = upd(m->fa);
+  if (e != cudaSuccess) {
+    fvh_device_mesh_destroy(dm);
+    return from_cuda(e);
+  }
+  *out = dm;
+  return FVH_OK;
+}
+
+const fvh_mesh_view *fvh_device_mesh_view(const fvh_device_mesh *dm) {
+  return dm ? &dm->view : nullptr;
+}
+
+void fvh_device_state_destroy(fvh_device_state *ds) {
+  if (!ds) return;
+  cudaFree(ds->base);
+  delete ds;
+}
+
+fvh_status fvh_device_state_create(int32_t dim, int32_t num_cells, fvh_device_state **out) {
+  if (!out || (dim != 2 && dim != 3) || num_cells <= 0) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  fvh_device_state *ds = new (std::nothrow) fvh_device_state();
+  if (!ds) return FVH_ERR_OUT_OF_MEMORY;
+  // planes padded to 64 doubles so each starts on a 512-byte boundary
+  const size_t stride = ((size_t)num_cells + 63) / 64 * 64;
+  const cudaError_t e = cudaMalloc(&ds->base, sizeof(double) * stride * (6 + dim));
+  if (e != cudaSuccess) {
+    delete ds;
+    return from_cuda(e);
+  }
+  double *b = ds->base;
+  ds->view.density = b;
+  b += stride;
+  for (int d = 0; d < dim; ++d, b += stride) ds->view.velocity[d] = b;
+  ds->view.internal_energy = b;
+  b += stride;
+  ds->view.pressure = b;
+  b += stride;
+  ds->view.temperature = b;
+  b += stride;
+  ds->view.sound_speed = b;
+  *out = ds;
+  return FVH_OK;
+}
+
+const fvh_state_view *fvh_device_state_view(const fvh_device_state *ds) {
+  return ds ? &ds->view : nullptr;
+}
+
+static void state_planes(const fvh_state_view *s, int dim, double **p) {
+  int k = 0;
+  p[k++] = s->density;
+  for (int d = 0; d < dim; ++d) p[k++] = s->velocity[d];
+  p[k++] = s->internal_energy;
+  p[k++] = s->pressure;
+  p[k++] = s->temperature;
+  p[k++] = s->sound_speed;
+}
+
+fvh_status fvh_state_upload(const fvh_state_view *dst, int32_t dim, int32_t num_cells,
+                            const double *host, fvh_stream_t stream) {
+  if (!state_ok(dst, dim) || !host || num_cells <= 0) return FVH_ERR_INVALID_ARGUMENT;
+  double *planes[9];
+  state_planes(dst, dim, planes);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 4 + dim && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(planes[k], host + (size_t)k * num_cells, sizeof(double) * num_cells,
+                        cudaMemcpyHostToDevice, cs(stream));
+  return from_cuda(e);
+}
+
+fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim, int32_t num_cells,
+                              double *host, fvh_stream_t stream) {
+  if (!state_ok(src, dim) || !host || num_cells <= 0) return FVH_ERR_INVALID_ARGUMENT;
+  double *planes[9];
+  state_planes(src, dim, planes);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 4 + dim && e == cudaSuccess; ++k)
+    e = cudaMemcpyAsync(host + (size_t)k * num_cells, planes[k], sizeof(double) * num_cells,
+                        cudaMemcpyDeviceToHost, cs(stream));
+  return from_cuda(e);
+}
+
+fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_state,
+                                   double *host_planes, int64_t nsteps, double *soln_time,
+                                   fvh_stream_t stream) {
+  if (!s || !state_ok(dev_state, s->mesh.dim) || !host_planes || !soln_time || nsteps < 0)
+    return FVH_ERR_INVALID_ARGUMENT;
+  const int D = s->mesh.dim, nc = s->mesh.num_cells;
+  cudaStream_t st = cs(stream);
+  s->host_scalars[1] = *soln_time;
+  cudaError_t e = cudaMemcpyAsync(s->scalars, s->host_scalars + 1, sizeof(double),
+                                  cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return from_cuda(e);
+  fvh_status r = fvh_state_upload(dev_state, D, nc, host_planes, stream);
+  for (int64_t k = 0; k < nsteps && r == FVH_OK; ++k) r = fvh_solver_step(s, dev_state, stream);
+  if (r == FVH_OK) r = fvh_state_download(dev_state, D, nc, host_planes, stream);
+  if (r != FVH_OK) return r;
+  double t = 0;
+  r = fvh_solver_check(s, stream, &t, nullptr);
+  *soln_time = t;
+  return r;
+}
+
+}  // extern "C"

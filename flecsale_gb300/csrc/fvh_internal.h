@@ -1,0 +1,25 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "flecsale_gb300.h"
+
+// Host mesh: topology and geometry arrays (see fvh_mesh.cpp for the rules).
+struct fvh_host_mesh {
+  int dim = 0, nc = 0, nf = 0, nv = 0;
+  std::vector<int32_t> face_cells;          // 2 per face
+  std::vector<int32_t> cf_off, cf;          // faces(c), signed
+  std::vector<int32_t> nb_off, nb;          // cell_vertex_neighbors(c)
+  std::vector<int32_t> cv_off, cv;          // vertices(c)
+  std::vector<int32_t> fv_off, fv;          // face -> vertices
+  std::vector<double> cc[3], cvol;          // cell centroid, volume
+  std::vector<double> fc[3], fn[3], fa;     // face centroid, normal, area
+  std::vector<double> vc[3];                // vertex coordinates
+};
+
+namespace fvh {
+fvh_status build_topology_and_geometry(fvh_host_mesh &m);
+double uniform01(uint64_t seed, uint64_t counter);
+}  // namespace fvh

@@ -1,0 +1,346 @@
+/*
+ * flecsale_gb300 — C ABI of the GB300 (sm_103a) Eulerian finite-volume hydro step.
+ *
+ * This header is the drop-in boundary for the hydro index tasks of FleCSALE's
+ * Eulerian solver (apps/hydro).  Each task entry point below replaces one FleCSI
+ * leaf task registered at apps/hydro/tasks.h:857-868 and launched from the time
+ * loop in apps/hydro/driver.h:317-413.  The reference passes FleCSI field
+ * accessors; this ABI passes plain structs of device pointers (one SoA plane per
+ * field component, the reference's "one array per field" registration of
+ * apps/hydro/driver.h:33-158) plus counts.  Nothing here uses C++ or CUDA types.
+ *
+ * Conventions
+ *  - All arrays named in fvh_mesh_view / fvh_state_view / fvh_gradient_view /
+ *    fvh_flux_view are caller-owned device memory (the fvh_device_* helpers can
+ *    allocate them).  Step calls never allocate.
+ *  - Every call is asynchronous and stream-ordered on the given stream; no call in
+ *    the time loop synchronises with the host.  Errors found by a kernel (the
+ *    reference's THROW_RUNTIME_ERROR at tasks.h:366-367 and tasks.h:654-655) are
+ *    recorded in a device status word (fvh_device_status) and read by the host
+ *    whenever it chooses; launch/argument errors are returned as fvh_status.
+ *  - Results are deterministic: no floating-point atomics are used anywhere; the
+ *    face-to-cell accumulation is a cell-centric gather in the cell's face order.
+ *  - dim is 2 or 3.  Index arrays are int32.
+ */
+#ifndef FLECSALE_GB300_H
+#define FLECSALE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FVH_ABI_VERSION 1
+
+/* A cudaStream_t; 0 is the legacy default stream. */
+typedef struct CUstream_st *fvh_stream_t;
+
+/* ------------------------------------------------------------------------- */
+/* Status codes                                                               */
+/* ------------------------------------------------------------------------- */
+typedef enum fvh_status {
+  FVH_OK = 0,
+  FVH_ERR_INVALID_ARGUMENT = 1,   /* null pointer, bad dim/kind, size mismatch   */
+  FVH_ERR_CUDA = 2,               /* a CUDA runtime call failed                  */
+  FVH_ERR_INFINITE_DT = 3,        /* tasks.h:366-367 "infinite delta t"          */
+  FVH_ERR_NEGATIVE_STATE = 4,     /* tasks.h:654-655 negative density or energy  */
+  FVH_ERR_UNSUPPORTED = 5,        /* mesh cell shape / option not supported      */
+  FVH_ERR_NO_DEVICE = 6,          /* no CUDA device visible                       */
+  FVH_ERR_OUT_OF_MEMORY = 7,
+  FVH_ERR_CAPACITY = 8            /* a request exceeds a fixed capacity           */
+} fvh_status;
+
+/* Human-readable text for an fvh_status value (static storage). */
+const char *fvh_status_string(int32_t status);
+
+/* ABI version of the loaded library (FVH_ABI_VERSION when built). */
+int32_t fvh_abi_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Physics / scheme parameters                                                */
+/* ------------------------------------------------------------------------- */
+typedef enum fvh_flux_kind {
+  FVH_FLUX_HLLE = 0,     /* reference default: flux_function -> hlle_flux,
+                            apps/hydro/types.h:118-125, flecsale/eqns/flux.h:79-106 */
+  FVH_FLUX_RUSANOV = 1,  /* flecsale/eqns/flux.h:51-65                               */
+  FVH_FLUX_HLLC = 2      /* not in the reference: Toro's HLLC with the HLLE
+                            wave-speed estimates (flux.h:82-86)                      */
+} fvh_flux_kind;
+
+typedef enum fvh_limiter_kind {
+  FVH_LIMITER_BARTH_JESPERSEN = 0, /* reference vertex limiter, tasks.h:267-299 */
+  FVH_LIMITER_NONE = 1             /* unlimited least-squares gradients         */
+} fvh_limiter_kind;
+
+typedef enum fvh_precision {
+  FVH_PRECISION_FP64 = 0,  /* everything in FP64 (reference arithmetic order)      */
+  FVH_PRECISION_MIXED = 1  /* FP32 reconstruction + Riemann flux, FP64 state,
+                              update, totals and dt                                */
+} fvh_precision;
+
+typedef struct fvh_params {
+  int32_t dim;            /* 2 or 3                                               */
+  int32_t flux_kind;      /* fvh_flux_kind (interior faces); walls use wall_flux  */
+  int32_t limiter;        /* fvh_limiter_kind                                     */
+  int32_t order;          /* 2 = MUSCL (reference); 1 = first order (zero grads)  */
+  int32_t recon_swap_ep;  /* 1 = reproduce the reference's reconstruction, which
+                             adds grad(e) to the face pressure and grad(p) to the
+                             face energy (tasks.h:429-430, 448-449); 0 = textbook */
+  int32_t precision;      /* fvh_precision                                        */
+  double gamma;           /* ideal gas ratio of specific heats (ideal_gas.h:42)   */
+  double cv;              /* specific heat at constant volume                      */
+  double cfl;             /* CFL number (inputs.h:64)                              */
+  double final_time;      /* dt is clamped to final_time - t (tasks.h:343,373)    */
+} fvh_params;
+
+/* Fill p with the reference's 2D shock-box defaults (apps/hydro/2d/inputs.cc:27-42):
+ * HLLE, Barth-Jespersen, 2nd order, swap on, FP64, gamma 1.4, cv 1, CFL 0.5, t_f 0.2. */
+void fvh_params_default(fvh_params *p, int32_t dim);
+
+/* ------------------------------------------------------------------------- */
+/* Views of device memory                                                     */
+/* ------------------------------------------------------------------------- */
+
+/* Mesh topology + geometry (burton mesh queries, apps/hydro/types.h:33 and the
+ * calls made in tasks.h).  Geometry is FP64, one plane per component. */
+typedef struct fvh_mesh_view {
+  int32_t dim;
+  int32_t num_cells;
+  int32_t num_faces;
+  int32_t num_vertices;
+  /* cells(f): face_cells[2f] = cells(f)[0], face_cells[2f+1] = cells(f)[1] or -1
+   * for a boundary face.  The face normal points out of cells(f)[0]. */
+  const int32_t *face_cells;
+  /* faces(c) in the reference's iteration order, CSR.  Each entry is f when
+   * c == cells(f)[0] (flux subtracted) and ~f (= -f-1) otherwise (flux added). */
+  const int32_t *cell_face_offsets;   /* [num_cells+1] */
+  const int32_t *cell_faces;
+  /* cell_vertex_neighbors(c) (tasks.h:190), CSR in the reference's order. */
+  const int32_t *cell_nbr_offsets;    /* [num_cells+1] */
+  const int32_t *cell_nbrs;
+  /* vertices(c) (tasks.h:270), CSR. */
+  const int32_t *cell_vertex_offsets; /* [num_cells+1] */
+  const int32_t *cell_vertices;
+  const double *cell_centroid[3];     /* c->centroid()   */
+  const double *cell_volume;          /* c->volume()     */
+  const double *face_centroid[3];     /* f->centroid()   */
+  const double *face_normal[3];       /* f->normal(), unit, out of cells(f)[0] */
+  const double *face_area;            /* f->area()       */
+  const double *vertex_coord[3];      /* v->coordinates() */
+} fvh_mesh_view;
+
+/* Cell state: the six hydro fields of driver.h:215-224 (d, v, e, p, T, a). */
+typedef struct fvh_state_view {
+  double *density;
+  double *velocity[3];
+  double *internal_energy;
+  double *pressure;
+  double *temperature;
+  double *sound_speed;
+} fvh_state_view;
+
+/* Limited cell gradients (driver.h:228-232); g[k] is d/dx_k.
+ * velocity[d][k] = d v_d / d x_k, the reference's grad_v(c)[d][k]. */
+typedef struct fvh_gradient_view {
+  double *density[3];
+  double *velocity[3][3];
+  double *internal_energy[3];
+  double *pressure[3];
+  double *sound_speed[3];
+} fvh_gradient_view;
+
+/* Area-scaled face fluxes (flux_data_t, driver.h:226): mass, momentum[dim], energy. */
+typedef struct fvh_flux_view {
+  double *mass;
+  double *momentum[3];
+  double *energy;
+} fvh_flux_view;
+
+/* Device status word.  Kernels record the first offending cell with an integer
+ * atomicMin on key = (cell << 8) | code, so the result does not depend on thread
+ * order.  FVH_STATUS_CLEAR means "no error".  Decode with fvh_status_decode. */
+typedef unsigned long long fvh_device_status;
+#define FVH_STATUS_CLEAR (~0ull)
+void fvh_status_decode(fvh_device_status s, int32_t *code, int64_t *cell);
+
+/* ------------------------------------------------------------------------- */
+/* Task entry points (stream-ordered, asynchronous, no allocation)            */
+/* ------------------------------------------------------------------------- */
+
+/* Bytes of device workspace fvh_evaluate_time_step needs for num_cells cells. */
+size_t fvh_time_step_workspace_bytes(int32_t num_cells);
+
+/* Replaces evaluate_time_step (tasks.h:331-376) plus the min-reduction over
+ * colours (driver.h:329-332): d_dt[0] = min(CFL / max_{c,f in c}
+ * (a_c + |v_c.n_f|) A_f / V_c, final_time - d_soln_time[0]).  A non-positive
+ * maximum records FVH_ERR_INFINITE_DT in d_status.  d_workspace must hold
+ * fvh_time_step_workspace_bytes(num_cells) bytes. */
+fvh_status fvh_evaluate_time_step(const fvh_mesh_view *mesh,
+                                  const fvh_state_view *state,
+                                  const fvh_params *params,
+                                  const double *d_soln_time, double *d_dt,
+                                  void *d_workspace, size_t workspace_bytes,
+                                  fvh_device_status *d_status,
+                                  fvh_stream_t stream);
+
+/* Replaces evaluate_gradients (tasks.h:145-321): vertex-neighbour least squares
+ * gradients of (d, v, e, p, a) with the Barth-Jespersen vertex limiter. */
+fvh_status fvh_evaluate_gradients(const fvh_mesh_view *mesh,
+                                  const fvh_state_view *state,
+                                  const fvh_gradient_view *grads,
+                                  const fvh_params *params,
+                                  fvh_stream_t stream);
+
+/* Replaces evaluate_fluxes (tasks.h:385-536): per face, reconstruct both sides at
+ * the face centroid, Riemann flux (interior) or wall flux (boundary), times area. */
+fvh_status fvh_evaluate_fluxes(const fvh_mesh_view *mesh,
+                               const fvh_state_view *state,
+                               const fvh_gradient_view *grads,
+                               const fvh_flux_view *flux,
+                               const fvh_params *params, fvh_stream_t stream);
+
+/* Replaces apply_update (tasks.h:589-659) and update_soln_time (tasks.h:545-576):
+ * delta_t = d_dt[0]*factor; d_soln_time[0] += delta_t; per cell
+ * du = sum over faces(c) of -/+ F_f, du *= delta_t / V_c, conservative update
+ * (euler_eqns.h:383-410) and EOS closure (euler_eqns.h:359-375).  A negative
+ * density or internal energy records FVH_ERR_NEGATIVE_STATE in d_status. */
+fvh_status fvh_apply_update(const fvh_mesh_view *mesh, const fvh_params *params,
+                            const double *d_dt, double factor,
+                            const fvh_flux_view *flux,
+                            const fvh_state_view *state, double *d_soln_time,
+                            fvh_device_status *d_status, fvh_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* Solver object: one mesh + its work buffers, the whole time step            */
+/* ------------------------------------------------------------------------- */
+typedef struct fvh_solver fvh_solver;
+
+/* Allocates gradients, fluxes, the dt workspace and the device scalars
+ * (solution time, dt, status) for a mesh already in device memory.  The mesh
+ * view is copied; the arrays it points to must outlive the solver. */
+fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params,
+                             fvh_solver **out);
+void fvh_solver_destroy(fvh_solver *s);
+
+/* One full time step of driver.h:325-375 on the state: dt reduction, then the
+ * predictor and the corrector (gradients -> fluxes -> update, factor 0.5 each). */
+fvh_status fvh_solver_step(fvh_solver *s, const fvh_state_view *state,
+                           fvh_stream_t stream);
+
+/* nsteps steps, stream-ordered.  With stop_at_final_time != 0 the host checks the
+ * solution time every check_every steps and stops once it reaches final_time
+ * (the dt clamp of tasks.h:373 makes the last step land on it). */
+fvh_status fvh_solver_run(fvh_solver *s, const fvh_state_view *state,
+                          int64_t nsteps, int32_t stop_at_final_time,
+                          int32_t check_every, int64_t *steps_done,
+                          fvh_stream_t stream);
+
+/* Device scalars owned by the solver. */
+double *fvh_solver_soln_time(fvh_solver *s);
+double *fvh_solver_dt(fvh_solver *s);
+fvh_device_status *fvh_solver_status(fvh_solver *s);
+const fvh_gradient_view *fvh_solver_gradients(fvh_solver *s);
+const fvh_flux_view *fvh_solver_fluxes(fvh_solver *s);
+
+/* Synchronises the stream, reads the status word and the solution time. */
+fvh_status fvh_solver_check(fvh_solver *s, fvh_stream_t stream,
+                            double *soln_time, int64_t *bad_cell);
+
+/* Reset the solution time to t and clear the status word (stream-ordered). */
+fvh_status fvh_solver_reset(fvh_solver *s, double t, fvh_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* Host mesh construction (the burton topology + geometry queries)            */
+/* ------------------------------------------------------------------------- */
+typedef struct fvh_host_mesh fvh_host_mesh;
+
+/* Build topology and geometry from cell -> vertex lists.
+ *  dim 2: each cell is a polygon with vertices listed counter-clockwise.
+ *  dim 3: each cell is a hexahedron (8 vertices, Exodus HEX8 order) or a
+ *         tetrahedron (4 vertices, Exodus TETRA4 order).
+ * vertex_coords is interleaved [num_vertices*dim]. */
+fvh_status fvh_host_mesh_create(int32_t dim, int32_t num_vertices,
+                                const double *vertex_coords, int32_t num_cells,
+                                const int32_t *cell_vertex_offsets,
+                                const int32_t *cell_vertices,
+                                fvh_host_mesh **out);
+
+/* Structured-origin box mesh stored unstructured: n[0] x n[1] (x n[2]) cells on
+ * [lo, hi], vertex and cell ids lexicographic with x fastest.  Interior vertices
+ * are moved by independent uniform offsets in [-jitter*h_k, +jitter*h_k] per axis
+ * (SplitMix64 stream keyed by seed and vertex id); boundary vertices stay put. */
+fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
+                             const double *hi, double jitter, uint64_t seed,
+                             fvh_host_mesh **out);
+
+void fvh_host_mesh_destroy(fvh_host_mesh *m);
+
+/* Host-memory view of the mesh arrays (valid while m lives). */
+fvh_status fvh_host_mesh_view(const fvh_host_mesh *m, fvh_mesh_view *out);
+
+/* Lengths of the CSR index arrays. */
+fvh_status fvh_host_mesh_nnz(const fvh_host_mesh *m, int64_t *cell_faces,
+                             int64_t *cell_nbrs, int64_t *cell_vertices);
+
+/* ------------------------------------------------------------------------- */
+/* Initial conditions (setup)                                                 */
+/* ------------------------------------------------------------------------- */
+typedef enum fvh_problem_kind {
+  FVH_PROBLEM_SHOCK_BOX = 0,   /* (0.125, 0, 0.1) where every x_k < 0, else (1, 0, 1):
+                                  apps/hydro/2d/inputs.cc:45-60, 3d/inputs.cc:120-137 */
+  FVH_PROBLEM_SOD = 1,         /* x < 0.5: (1, 0, 1); else (0.125, 0, 0.1)             */
+  FVH_PROBLEM_FOUR_QUADRANT = 2, /* 2D quadrants about (0.5, 0.5), (d, u, v, p):
+                                  NE (1.5,0,0,1.5) NW (0.5323,1.206,0,0.3)
+                                  SW (0.138,1.206,1.206,0.029) SE (0.5323,0,1.206,0.3) */
+  FVH_PROBLEM_INNER_CUBE = 3,  /* every x_k < 0.5: (1, 0, 1); else (0.125, 0, 0.1)     */
+  FVH_PROBLEM_KELVIN_HELMHOLTZ = 4, /* d = 2 (|y-0.5| < 0.25) else 1, u = +0.5 / -0.5,
+                                  v = 0.01 sin(4 pi x) + 1e-3 U[-1,1) (seeded), p = 2.5 */
+  FVH_PROBLEM_UNIFORM = 5      /* (1, 0, 1) everywhere                                  */
+} fvh_problem_kind;
+
+/* Per-cell (d, v, p) of the problem at the cell centroid, closed with the ideal
+ * gas (update_state_from_pressure, euler_eqns.h:333-350).  host_planes receives
+ * 6+dim planes of num_cells doubles: d, v[0..dim), e, p, T, a. */
+fvh_status fvh_host_initial_state(int32_t kind, const fvh_host_mesh *m,
+                                  const fvh_params *p, uint64_t seed,
+                                  double *host_planes);
+
+/* ------------------------------------------------------------------------- */
+/* Device memory helpers (setup only, never called inside a step)             */
+/* ------------------------------------------------------------------------- */
+typedef struct fvh_device_mesh fvh_device_mesh;
+
+/* Copy a host mesh to device memory. */
+fvh_status fvh_device_mesh_create(const fvh_host_mesh *m, fvh_device_mesh **out);
+void fvh_device_mesh_destroy(fvh_device_mesh *dm);
+const fvh_mesh_view *fvh_device_mesh_view(const fvh_device_mesh *dm);
+
+/* State planes for num_cells cells in one device allocation. */
+typedef struct fvh_device_state fvh_device_state;
+fvh_status fvh_device_state_create(int32_t dim, int32_t num_cells,
+                                   fvh_device_state **out);
+void fvh_device_state_destroy(fvh_device_state *ds);
+const fvh_state_view *fvh_device_state_view(const fvh_device_state *ds);
+
+/* Host <-> device copies of a whole state.  Host layout: 6+dim planes of
+ * num_cells doubles in the order d, v[0..dim), e, p, T, a. */
+fvh_status fvh_state_upload(const fvh_state_view *dst, int32_t dim,
+                            int32_t num_cells, const double *host_planes,
+                            fvh_stream_t stream);
+fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim,
+                              int32_t num_cells, double *host_planes,
+                              fvh_stream_t stream);
+
+/* End-to-end call for callers that hold the state in host memory: upload the
+ * state, advance nsteps time steps, download it, then synchronise.  Solution
+ * time in/out through *soln_time. */
+fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_state,
+                                   double *host_planes, int64_t nsteps,
+                                   double *soln_time, fvh_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLECSALE_GB300_H */

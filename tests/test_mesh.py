@@ -1,0 +1,94 @@
+"""Topology and geometry of the host mesh builder (the burton queries the hydro
+tasks use: cells(f), faces(c), cell_vertex_neighbors(c), vertices(c), centroids,
+volumes, face normals and areas)."""
+import numpy as np
+import pytest
+
+import flecsale_gb300.hydro as H
+
+
+def _closure(m):
+    """Sum over faces(c) of +-A_f n_f must vanish for a closed cell."""
+    a = m.arrays()
+    off, cf = a["cell_face_offsets"], a["cell_faces"]
+    s = np.zeros((m.dim, m.num_cells))
+    for c in range(m.num_cells):
+        for q in range(off[c], off[c + 1]):
+            f = cf[q]
+            sign = 1.0 if f >= 0 else -1.0
+            f = f if f >= 0 else ~f
+            s[:, c] += sign * a["face_area"][f] * a["face_normal"][:, f]
+    return s
+
+
+@pytest.mark.parametrize("dim,n,jit", [(2, (9, 7), 0.0), (2, (9, 7), 0.2), (3, (5, 4, 3), 0.0), (3, (5, 4, 3), 0.15)])
+def test_box_mesh_invariants(fvh, dim, n, jit):
+    m = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, jit, 4)
+    a = m.arrays()
+    nc = int(np.prod(n))
+    assert m.num_cells == nc
+    assert m.num_vertices == int(np.prod([k + 1 for k in n]))
+    if dim == 2:
+        nfaces = (n[0] + 1) * n[1] + n[0] * (n[1] + 1)
+    else:
+        nfaces = ((n[0] + 1) * n[1] * n[2] + n[0] * (n[1] + 1) * n[2] + n[0] * n[1] * (n[2] + 1))
+    assert m.num_faces == nfaces
+    np.testing.assert_allclose(a["cell_volume"].sum(), 1.0, rtol=1e-12)
+    assert np.all(a["cell_volume"] > 0)
+    np.testing.assert_allclose(np.linalg.norm(a["face_normal"], axis=0), 1.0, rtol=1e-14)
+    assert np.abs(_closure(m)).max() < 1e-14
+    fc = a["face_cells"]
+    assert np.all(fc[:, 0] >= 0) and np.all((fc[:, 1] == -1) | (fc[:, 1] > fc[:, 0]))
+    # normals point out of cells(f)[0]
+    d = a["face_centroid"] - a["cell_centroid"][:, fc[:, 0]]
+    assert np.all(np.sum(d * a["face_normal"], axis=0) > 0)
+    # faces get ids in order of first encounter (cell order, then local order)
+    first = []
+    seen = set()
+    for c in range(nc):
+        for q in range(a["cell_face_offsets"][c], a["cell_face_offsets"][c + 1]):
+            f = a["cell_faces"][q]
+            f = f if f >= 0 else ~f
+            if f not in seen:
+                seen.add(f)
+                first.append(f)
+    assert first == list(range(m.num_faces))
+    # vertex neighbours: all cells sharing a vertex, ascending, no self
+    cv = [set(a["cell_vertices"][a["cell_vertex_offsets"][c]:a["cell_vertex_offsets"][c + 1]]) for c in range(nc)]
+    for c in range(0, nc, max(1, nc // 13)):
+        got = list(a["cell_nbrs"][a["cell_nbr_offsets"][c]:a["cell_nbr_offsets"][c + 1]])
+        exp = sorted(k for k in range(nc) if k != c and cv[k] & cv[c])
+        assert got == exp
+    # boundary vertices stay on the boundary
+    vc = a["vertex_coord"]
+    assert vc.min() == 0.0 and vc.max() == 1.0
+
+
+def test_jitter_is_seeded_and_bounded(fvh):
+    a = H.HostMesh.box(2, (20, 20), [0, 0], [1, 1], 0.2, 1).arrays()["vertex_coord"]
+    b = H.HostMesh.box(2, (20, 20), [0, 0], [1, 1], 0.2, 1).arrays()["vertex_coord"]
+    c = H.HostMesh.box(2, (20, 20), [0, 0], [1, 1], 0.2, 2).arrays()["vertex_coord"]
+    u = H.HostMesh.box(2, (20, 20), [0, 0], [1, 1], 0.0, 1).arrays()["vertex_coord"]
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert np.abs(a - u).max() <= 0.2 / 20 + 1e-15 and np.abs(a - u).max() > 0.15 / 20
+
+
+def test_affine_centroids(fvh):
+    """Polygon/hex centroid and volume are exact for affine cells."""
+    m = H.HostMesh.box(2, (3, 2), [0, 0], [3, 1], 0.0, 0)
+    np.testing.assert_allclose(m.arrays()["cell_centroid"][:, 0], [0.5, 0.25], atol=1e-15)
+    m = H.HostMesh.box(3, (2, 2, 2), [0, 0, 0], [2, 4, 6], 0.0, 0)
+    a = m.arrays()
+    np.testing.assert_allclose(a["cell_volume"], 6.0, rtol=1e-14)
+    np.testing.assert_allclose(a["cell_centroid"][:, 0], [0.5, 1.0, 1.5], rtol=1e-14)
+
+
+def test_tet_mesh(fvh):
+    """Two tetrahedra sharing a face (Exodus TETRA4 order)."""
+    x = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1]], float)
+    cells = np.array([0, 1, 2, 3, 1, 2, 3, 4][:4] + [1, 4, 2, 3], np.int32)
+    m = H.HostMesh.from_cells(3, x, np.array([0, 4, 8], np.int32), cells)
+    a = m.arrays()
+    assert m.num_faces == 7
+    assert np.sum(a["face_cells"][:, 1] >= 0) == 1
+    np.testing.assert_allclose(a["cell_volume"][0], 1 / 6, rtol=1e-14)
