@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Benchmark: zone-updates/s of the Eulerian MUSCL hydro step on GB300.
+
+Workload (one bench step = one full time step: CFL dt reduction + predictor +
+corrector, apps/hydro/driver.h:325-375): 2D four-quadrant Riemann problem on a
+1024x1024 quad mesh over [0,1]^2, interior nodes jittered by a seeded uniform
++-0.2h (seed 1), stored unstructured; ideal gas gamma 1.4; second-order MUSCL
+with least-squares vertex-neighbour gradients and the reference's
+Barth-Jespersen vertex limiter; HLLC fluxes; CFL 0.4.  Synthetic data.
+
+The headline value is the mixed-precision form (FP32 reconstruction + flux,
+FP64 state/update/dt); the plain FP64 path is reported beside it with the
+relative L1 density/energy error of mixed vs FP64 after the same steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (torchrun) runs one independent replica per GPU (the single-mesh step is
+not sharded): value = all ranks' zone-updates / max-over-ranks time.
+--impl reference times the CPU restatement of the reference solver (the
+reference itself cannot be built) with all host threads, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "zone-updates/s on 1 GB300: FP64 plain vs mixed/batched at ≤1e-4 L1; p50/p99"
+UNIT = "zone-updates/s"
+N_SIDE = 1024
+JITTER, SEED = 0.2, 1
+WORKLOAD = ("2D four-quadrant Riemann problem, 1024x1024 quads on [0,1]^2 jittered "
+            "+-0.2h (seed 1), gamma 1.4, MUSCL LSQ + Barth-Jespersen vertex limiter, "
+            "HLLC, CFL 0.4, one step = dt + predictor + corrector")
+
+
+def build_problem():
+    import flecsale_gb300.hydro as H
+    mesh = H.HostMesh.box(2, (N_SIDE, N_SIDE), [0, 0], [1, 1], JITTER, SEED)
+    kw = dict(flux="hllc", limiter="barth_jespersen", order=2, swap=True, cfl=0.4,
+              final_time=1.0e9)
+    p64 = H.make_params(2, precision="fp64", **kw)
+    p32 = H.make_params(2, precision="mixed", **kw)
+    state0 = H.initial_state("four_quadrant", mesh, p64)
+    return H, mesh, p64, p32, state0
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per launch (each array a kernel must touch, moved once)
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(mesh, precision: str) -> dict:
+    D = mesh.dim
+    nc, nf, nv = mesh.num_cells, mesh.num_faces, mesh.num_vertices
+    ncf, nnb, ncv = mesh.nnz_faces, mesh.nnz_nbrs, mesh.nnz_vertices
+    csr_cf = 4 * (nc + 1) + 4 * ncf
+    csr_nb = 4 * (nc + 1) + 4 * nnb
+    csr_cv = 4 * (nc + 1) + 4 * ncv
+    if precision == "fp64":
+        return {
+            "dt": nc * (8 * (1 + D) + 8) + csr_cf + nf * (8 * D + 8),
+            "gradients": 8 * (D + 4) * nc + 8 * D * nc + 8 * D * nv + csr_nb + csr_cv
+                         + 8 * D * (D + 4) * nc,
+            "fluxes": 8 * nf + 8 * D * nf * 2 + 8 * nf + 8 * (D + 2) * nf
+                      + 8 * (D + 4) * nc + 8 * D * (D + 4) * nc + 8 * D * nc,
+            "update": csr_cf + 8 * (D + 2) * nf + 8 * nc + 8 * (D + 2) * nc + 8 * (D + 5) * nc,
+        }
+    cen4 = 1 if D == 2 else 2
+    grad4 = 3 if D == 2 else 6
+    fdx4 = 1 if D == 2 else 2
+    return {
+        "pack_dt": 8 * (D + 4) * nc + 32 * nc + 8 * nc + csr_cf + 16 * nf,
+        "dt_final": 8 * 1216,
+        "gradients": 32 * nc + 16 * cen4 * (nc + nv) + csr_nb + csr_cv + 16 * grad4 * nc,
+        # mean of the predictor (writes the next FP32 pack) and the corrector
+        "flux_update": 32 * nc + 16 * grad4 * nc + csr_cf + 8 * nf + 16 * nf + 16 * fdx4 * nf
+                       + 8 * nc + 8 * (D + 2) * nc + 8 * (D + 5) * nc + 16 * nc,
+    }
+
+
+def per_zone_update_bytes(mesh, precision: str) -> float:
+    b = algorithmic_bytes(mesh, precision)
+    if precision == "fp64":
+        tot = b["dt"] + 2 * (b["gradients"] + b["fluxes"] + b["update"])
+    else:
+        tot = b["pack_dt"] + b["dt_final"] + 2 * (b["gradients"] + b["flux_update"])
+    return tot / mesh.num_cells
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic() -> dict:
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.proc, self.out = gpu, None, None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self) -> dict:
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (C++ restatement of the reference, OpenMP)
+# ---------------------------------------------------------------------------
+def cpu_baseline(mesh, params, state0, budget_s: float = 8.0, max_steps: int = 40) -> dict:
+    import oracle
+    from tests import _util as U
+    O = oracle.load()
+    s = state0.copy()
+    U.oracle_run(O, mesh, s, params, 1)  # warm-up step
+    n, t0 = 0, time.perf_counter()
+    while n < max_steps and (time.perf_counter() - t0) < budget_s:
+        U.oracle_run(O, mesh, s, params, 1)
+        n += 1
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": mesh.num_cells * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} full time steps of the {N_SIDE}x{N_SIDE} workload in {dt:.1f} s "
+                      f"(FP64, HLLC; oracle/hydro_oracle.cpp, -O2, OpenMP)"}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(backend: str):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+        return dist, ws, rank, local
+    return None, 1, 0, local
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    H, mesh, p64, _, state0 = build_problem()
+    import oracle
+    from tests import _util as U
+    O = oracle.load()
+    s = state0.copy()
+    for _ in range(args.warmup):
+        U.oracle_run(O, mesh, s, p64, 1)
+    t0 = time.perf_counter()
+    U.oracle_run(O, mesh, s, p64, args.steps)
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    value = mesh.num_cells * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": mesh.num_cells, "faces": mesh.num_faces,
+                   "form": "reference CPU solver restated (oracle), FP64"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full time steps of the workload, all host threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def timed_steps(torch, solver, dstate, stream, K, dist):
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        solver.step(dstate, stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    return ms
+
+
+def run_ours(args):
+    import torch
+    dist, ws, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    H, mesh, p64, p32, state0 = build_problem()
+    stream = torch.cuda.Stream()
+    dmesh = H.DeviceMesh(mesh)
+    nc = mesh.num_cells
+    results = {}
+    finals = {}
+    with ClockSampler(local) as clk:
+        for form, params in (("mixed", p32), ("fp64", p64)):
+            dstate = H.DeviceState(2, nc)
+            solver = H.Solver(dmesh, params)
+            dstate.upload(state0, stream)
+            solver.reset(0.0, stream)
+            for _ in range(args.warmup):
+                solver.step(dstate, stream)
+            ms = timed_steps(torch, solver, dstate, stream, args.steps, dist)
+            code, t, cell = solver.status(stream)
+            if code != 0:
+                raise RuntimeError(f"{form}: device status {code} at cell {cell}")
+            finals[form] = dstate.download(stream)
+            results[form] = {"ms": ms, "launches": solver.launches_per_step(), "t": t,
+                             "solver": solver, "state": dstate}
+    clocks = clk.summary()
+
+    # end to end through the C ABI with host buffers (mixed form)
+    r = results["mixed"]
+    host = torch.empty((7, nc), dtype=torch.float64, pin_memory=True).numpy()
+    host[:] = state0[:7]
+    t_sim = 0.0
+    for _ in range(args.warmup):
+        t_sim = r["solver"].advance_host(r["state"], host, 1, t_sim, stream)
+    if dist:
+        dist.barrier()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        t_sim = r["solver"].advance_host(r["state"], host, 1, t_sim, stream)
+    e2e_s = time.perf_counter() - w0
+    if dist:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    # per-kernel timings (CUDA events between launches on the stream)
+    prof = {f: results[f]["solver"].profile(results[f]["state"], 10, stream) for f in results}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    hbm, peak_kind = peaks()
+    traffic = ncu_traffic()
+
+    def roofline(form):
+        ab = algorithmic_bytes(mesh, form)
+        p = prof[form]
+        dom = max(p, key=lambda k: p[k][0] * p[k][1])
+        achieved = ab[dom] / (p[dom][0] * 1e-3) / 1e9
+        step_ms = sum(v[0] * v[1] for v in p.values())
+        return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
+                "traffic": traffic.get(f"{form}:{dom}"),
+                "algorithmic_bytes_per_launch": ab[dom],
+                "kernels": {k: {"mean_ms": v[0], "launches_per_step": v[1],
+                                "share": v[0] * v[1] / step_ms,
+                                "achieved_gbs": ab[k] / (v[0] * 1e-3) / 1e9}
+                            for k, v in p.items()}}
+
+    zu = lambda ms: ws * nc * args.steps / (ms * 1e-3)
+    m, f = finals["mixed"], finals["fp64"]
+    l1 = lambda a, b: float(np.abs(a - b).sum() / np.abs(b).sum())
+    E = lambda s: s[0] * (s[3] + 0.5 * (s[1] ** 2 + s[2] ** 2))
+    st_bytes = 7 * 8 * nc
+    line = {
+        "metric": METRIC,
+        "value": zu(results["mixed"]["ms"]),
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": results["mixed"]["ms"] / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": nc, "faces": mesh.num_faces,
+                   "form": "mixed: FP32 reconstruction + Riemann flux, FP64 state/update/dt",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                   "l2": "no flush: per-step working set (state, FP32 pack/gradients, mesh) "
+                         f"~{per_zone_update_bytes(mesh, 'mixed') * nc / 2 / 1e6:.0f} MB per stage > 129 MB L2",
+                   "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "mixed")},
+        "clocks": clocks,
+        "e2e": {"value": ws * nc * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": st_bytes, "d2h_bytes_per_step": st_bytes,
+                "call": "fvh_solver_advance_host (host state in, 1 step, host state out)"},
+        "gpu_launches": results["mixed"]["launches"] * args.steps,
+        "roofline": roofline("mixed"),
+        "plain_fp64": {"value": zu(results["fp64"]["ms"]),
+                       "ms_per_step": results["fp64"]["ms"] / args.steps,
+                       "gpu_launches": results["fp64"]["launches"] * args.steps,
+                       "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "fp64"),
+                       "roofline": roofline("fp64")},
+        "mixed_over_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
+        "accuracy": {"steps": args.warmup + args.steps,
+                     "l1_density_mixed_vs_fp64": l1(m[0], f[0]),
+                     "l1_total_energy_mixed_vs_fp64": l1(E(m), E(f)),
+                     "linf_density_mixed_vs_fp64": float(np.abs(m[0] - f[0]).max())},
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(mesh, p64, state0)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -31,7 +31,7 @@ UNITS = [
     ("fvh_mesh.cpp", []),
     ("fvh_problems.cpp", []),
     ("fvh_plain.cu", ["--fmad=false"]),
-    ("fvh_mixed.cu", []),
+    ("fvh_mixed.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("fvh_capi.cu", []),
 ]
 

@@ -294,25 +294,99 @@ fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params
 }
 
 static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state,
-                                      cudaStream_t st) {
+                                      cudaStream_t st,
+                                      const fvh::mixed::launch_mark &mark = {}) {
   const fvh_mesh_view &m = s->mesh;
   const fvh_params &p = s->params;
   double *t = s->scalars, *dt = s->scalars + 1, *partial = s->scalars + 2;
   if (p.precision == FVH_PRECISION_MIXED)
     return from_cuda(fvh::mixed::step(s->mixed, m, p, *state, t, dt, partial,
-                                      dt_blocks(m.num_cells), s->status, st));
+                                      dt_blocks(m.num_cells), s->status, st, mark));
   const size_t wsb = fvh_time_step_workspace_bytes(m.num_cells);
-  fvh_status r = fvh_evaluate_time_step(&m, state, &p, t, dt, partial, wsb, s->status,
-                                        reinterpret_cast<fvh_stream_t>(st));
+  const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
+  fvh_status r = fvh_evaluate_time_step(&m, state, &p, t, dt, partial, wsb, s->status, fs);
+  mark("dt");
   for (int stage = 0; stage < 2 && r == FVH_OK; ++stage) {
-    r = fvh_evaluate_gradients(&m, state, &s->grads, &p, reinterpret_cast<fvh_stream_t>(st));
-    if (r == FVH_OK)
-      r = fvh_evaluate_fluxes(&m, state, &s->grads, &s->flux, &p,
-                              reinterpret_cast<fvh_stream_t>(st));
-    if (r == FVH_OK)
-      r = fvh_apply_update(&m, &p, dt, 0.5, &s->flux, state, t, s->status,
-                           reinterpret_cast<fvh_stream_t>(st));
+    r = fvh_evaluate_gradients(&m, state, &s->grads, &p, fs);
+    mark("gradients");
+    if (r == FVH_OK) r = fvh_evaluate_fluxes(&m, state, &s->grads, &s->flux, &p, fs);
+    mark("fluxes");
+    if (r == FVH_OK) r = fvh_apply_update(&m, &p, dt, 0.5, &s->flux, state, t, s->status, fs);
+    mark("update");
   }
+  return r;
+}
+
+int32_t fvh_solver_launches_per_step(const fvh_solver *s) {
+  if (!s) return 0;
+  if (s->params.precision == FVH_PRECISION_MIXED) return fvh::mixed::launches_per_step(s->params);
+  // dt (partial + final) + per stage: gradients (or D*(D+4) memsets), fluxes, update
+  const int D = s->mesh.dim;
+  const int grad = s->params.order == 1 ? D * (D + 4) : 1;
+  return 2 + 2 * (grad + 2);
+}
+
+namespace {
+struct profile_ctx {
+  cudaStream_t st;
+  std::vector<cudaEvent_t> events;
+  std::vector<const char *> names;
+  size_t next = 0;
+};
+void profile_mark(void *vctx, const char *name) {
+  profile_ctx *c = static_cast<profile_ctx *>(vctx);
+  if (c->next < c->events.size()) {
+    cudaEventRecord(c->events[c->next], c->st);
+    c->names.push_back(name);
+  }
+  c->next++;
+}
+}  // namespace
+
+fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_t nsteps,
+                              int32_t max_kernels, const char **names, double *mean_ms,
+                              int32_t *launches_per_step, int32_t *nkernels,
+                              fvh_stream_t stream) {
+  if (!s || !state_ok(state, s->mesh.dim) || nsteps <= 0 || max_kernels <= 0 || !names ||
+      !mean_ms || !launches_per_step || !nkernels)
+    return FVH_ERR_INVALID_ARGUMENT;
+  profile_ctx ctx;
+  ctx.st = cs(stream);
+  const size_t nev = (size_t)nsteps * 16 + 1;
+  ctx.events.resize(nev);
+  for (auto &e : ctx.events) cudaEventCreate(&e);
+  fvh::mixed::launch_mark mark;
+  mark.fn = profile_mark;
+  mark.ctx = &ctx;
+  fvh_status r = FVH_OK;
+  profile_mark(&ctx, "");  // start event
+  for (int k = 0; k < nsteps && r == FVH_OK; ++k) r = solver_step_enqueue(s, state, ctx.st, mark);
+  if (r == FVH_OK) r = from_cuda(cudaStreamSynchronize(ctx.st));
+  int32_t nk = 0;
+  if (r == FVH_OK) {
+    std::vector<double> total(max_kernels, 0.0);
+    std::vector<int> count(max_kernels, 0);
+    const size_t recorded = ctx.names.size();
+    for (size_t i = 1; i < recorded; ++i) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ctx.events[i - 1], ctx.events[i]);
+      int k = 0;
+      for (; k < nk; ++k)
+        if (std::strcmp(names[k], ctx.names[i]) == 0) break;
+      if (k == nk) {
+        if (nk == max_kernels) continue;
+        names[nk++] = ctx.names[i];
+      }
+      total[k] += ms;
+      count[k]++;
+    }
+    for (int k = 0; k < nk; ++k) {
+      mean_ms[k] = count[k] ? total[k] / count[k] : 0.0;
+      launches_per_step[k] = count[k] / nsteps;
+    }
+  }
+  *nkernels = nk;
+  for (auto &e : ctx.events) cudaEventDestroy(e);
   return r;
 }
 
@@ -493,7 +567,7 @@ fvh_status fvh_device_state_create(int32_t dim, int32_t num_cells, fvh_device_st
   if (!ds) return FVH_ERR_OUT_OF_MEMORY;
   // planes padded to 64 doubles so each starts on a 512-byte boundary
   const size_t stride = ((size_t)num_cells + 63) / 64 * 64;
-  const cudaError_t e = cudaMalloc(&ds->base, sizeof(double) * stride * (6 + dim));
+  const cudaError_t e = cudaMalloc(&ds->base, sizeof(double) * stride * (5 + dim));
   if (e != cudaSuccess) {
     delete ds;
     return from_cuda(e);
@@ -533,7 +607,7 @@ fvh_status fvh_state_upload(const fvh_state_view *dst, int32_t dim, int32_t num_
   double *planes[9];
   state_planes(dst, dim, planes);
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < 4 + dim && e == cudaSuccess; ++k)
+  for (int k = 0; k < 5 + dim && e == cudaSuccess; ++k)
     e = cudaMemcpyAsync(planes[k], host + (size_t)k * num_cells, sizeof(double) * num_cells,
                         cudaMemcpyHostToDevice, cs(stream));
   return from_cuda(e);
@@ -545,7 +619,7 @@ fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim, int32_t nu
   double *planes[9];
   state_planes(src, dim, planes);
   cudaError_t e = cudaSuccess;
-  for (int k = 0; k < 4 + dim && e == cudaSuccess; ++k)
+  for (int k = 0; k < 5 + dim && e == cudaSuccess; ++k)
     e = cudaMemcpyAsync(host + (size_t)k * num_cells, planes[k], sizeof(double) * num_cells,
                         cudaMemcpyDeviceToHost, cs(stream));
   return from_cuda(e);

@@ -132,6 +132,10 @@ def _declare(L: C.CDLL) -> None:
         "fvh_state_download": (C.c_int, [C.POINTER(StateView), C.c_int32, C.c_int32, _dp, vp]),
         "fvh_solver_advance_host": (C.c_int, [vp, C.POINTER(StateView), _dp, C.c_int64,
                                               C.POINTER(C.c_double), vp]),
+        "fvh_solver_launches_per_step": (C.c_int32, [vp]),
+        "fvh_solver_profile": (C.c_int, [vp, C.POINTER(StateView), C.c_int32, C.c_int32,
+                                         C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -270,8 +274,8 @@ class HostMesh:
 
 
 def initial_state(kind: str, mesh: HostMesh, params: Params, seed: int = 0) -> np.ndarray:
-    """(6+dim, num_cells) FP64 planes d, v..., e, p, T, a."""
-    out = np.empty((6 + mesh.dim, mesh.num_cells), np.float64)
+    """(5+dim, num_cells) FP64 planes d, v..., e, p, T, a."""
+    out = np.empty((5 + mesh.dim, mesh.num_cells), np.float64)
     check(lib().fvh_host_initial_state(PROBLEM[kind], mesh._h, C.byref(params),
                                        C.c_uint64(seed), _dptr(out)), "fvh_host_initial_state")
     return out
@@ -349,7 +353,7 @@ class DeviceState:
                                      _dptr(planes), stream_handle(stream)), "fvh_state_upload")
 
     def download(self, stream=None) -> np.ndarray:
-        out = np.empty((6 + self.dim, self.num_cells), np.float64)
+        out = np.empty((5 + self.dim, self.num_cells), np.float64)
         check(lib().fvh_state_download(C.byref(self.view), self.dim, self.num_cells,
                                        _dptr(out), stream_handle(stream)), "fvh_state_download")
         return out
@@ -401,6 +405,20 @@ class Solver:
                                             nsteps, C.byref(tt), stream_handle(stream)),
               "fvh_solver_advance_host")
         return tt.value
+
+    def launches_per_step(self) -> int:
+        return lib().fvh_solver_launches_per_step(self._h)
+
+    def profile(self, state: DeviceState, nsteps: int, stream=None) -> dict:
+        """{kernel name: (mean ms per launch, launches per step)}."""
+        mx = 16
+        names = (C.c_char_p * mx)()
+        ms = np.zeros(mx)
+        per = (C.c_int32 * mx)()
+        nk = C.c_int32()
+        check(lib().fvh_solver_profile(self._h, C.byref(state.view), nsteps, mx, names, _dptr(ms),
+                                       per, C.byref(nk), stream_handle(stream)), "fvh_solver_profile")
+        return {names[k].decode(): (float(ms[k]), int(per[k])) for k in range(nk.value)}
 
     @property
     def d_soln_time(self) -> int:

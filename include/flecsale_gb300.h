@@ -244,6 +244,19 @@ fvh_device_status *fvh_solver_status(fvh_solver *s);
 const fvh_gradient_view *fvh_solver_gradients(fvh_solver *s);
 const fvh_flux_view *fvh_solver_fluxes(fvh_solver *s);
 
+/* Kernel launches one fvh_solver_step makes (the CUDA graph's node count). */
+int32_t fvh_solver_launches_per_step(const fvh_solver *s);
+
+/* Profiling run: nsteps steps launched kernel by kernel with a CUDA event
+ * recorded on the stream after every launch.  For each distinct kernel name
+ * (at most max_kernels) returns its static name, its mean duration in
+ * milliseconds per launch and its launches per step.  Synchronises. */
+fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state,
+                              int32_t nsteps, int32_t max_kernels,
+                              const char **names, double *mean_ms,
+                              int32_t *launches_per_step, int32_t *nkernels,
+                              fvh_stream_t stream);
+
 /* Synchronises the stream, reads the status word and the solution time. */
 fvh_status fvh_solver_check(fvh_solver *s, fvh_stream_t stream,
                             double *soln_time, int64_t *bad_cell);
@@ -302,7 +315,7 @@ typedef enum fvh_problem_kind {
 
 /* Per-cell (d, v, p) of the problem at the cell centroid, closed with the ideal
  * gas (update_state_from_pressure, euler_eqns.h:333-350).  host_planes receives
- * 6+dim planes of num_cells doubles: d, v[0..dim), e, p, T, a. */
+ * 5+dim planes of num_cells doubles: d, v[0..dim), e, p, T, a. */
 fvh_status fvh_host_initial_state(int32_t kind, const fvh_host_mesh *m,
                                   const fvh_params *p, uint64_t seed,
                                   double *host_planes);
@@ -324,7 +337,7 @@ fvh_status fvh_device_state_create(int32_t dim, int32_t num_cells,
 void fvh_device_state_destroy(fvh_device_state *ds);
 const fvh_state_view *fvh_device_state_view(const fvh_device_state *ds);
 
-/* Host <-> device copies of a whole state.  Host layout: 6+dim planes of
+/* Host <-> device copies of a whole state.  Host layout: 5+dim planes of
  * num_cells doubles in the order d, v[0..dim), e, p, T, a. */
 fvh_status fvh_state_upload(const fvh_state_view *dst, int32_t dim,
                             int32_t num_cells, const double *host_planes,

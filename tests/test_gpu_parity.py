@@ -20,11 +20,14 @@ CASES = [
     (2, (24, 17), 0.2, "four_quadrant", "hllc", "barth_jespersen", 2, True),
     (2, (24, 17), 0.2, "four_quadrant", "hlle", "barth_jespersen", 2, True),
     (2, (24, 17), 0.2, "kelvin_helmholtz", "rusanov", "barth_jespersen", 2, False),
-    (2, (24, 17), 0.2, "sod", "hllc", "none", 2, True),
+    (2, (24, 17), 0.2, "four_quadrant", "hllc", "none", 2, True),
+    (2, (24, 17), 0.2, "kelvin_helmholtz", "hlle", "none", 2, False),
+    (2, (24, 17), 0.2, "sod", "hllc", "barth_jespersen", 2, True),
     (2, (24, 17), 0.0, "sod", "hllc", "barth_jespersen", 1, True),
     (3, (7, 6, 5), 0.15, "inner_cube", "rusanov", "barth_jespersen", 2, True),
     (3, (7, 6, 5), 0.15, "inner_cube", "hlle", "barth_jespersen", 2, True),
-    (3, (7, 6, 5), 0.15, "inner_cube", "hllc", "none", 2, False),
+    (3, (7, 6, 5), 0.15, "kelvin_helmholtz", "hllc", "none", 2, False),
+    (3, (7, 6, 5), 0.15, "inner_cube", "hllc", "barth_jespersen", 1, True),
 ]
 
 
@@ -34,7 +37,8 @@ def _setup(cuda, dim, n, jitter, problem, flux, limiter, order, swap, warm_steps
     state = H.initial_state(problem, mesh, p, seed=11)
     O = __import__("oracle").load()
     # advance a little on the oracle so gradients and limiters are active
-    U.oracle_run(O, mesh, state, p, warm_steps)
+    st, _, _ = U.oracle_run(O, mesh, state, p, warm_steps)
+    assert st == 0 and np.all(np.isfinite(state[:5 + dim]))
     return mesh, p, state, O
 
 
@@ -76,12 +80,12 @@ def test_tasks_bitwise(cuda, case):
     st, dt = U.oracle_time_step(O, mesh, state, p, 0.05)
     assert st == 0 and dt_gpu == dt
     g = U.oracle_gradients(O, mesh, state, p)
-    assert np.array_equal(g_gpu, g)
+    assert np.array_equal(g_gpu, g, equal_nan=True)
     f = U.oracle_fluxes(O, mesh, state, g, p)
-    assert np.array_equal(f_gpu, f)
+    assert np.array_equal(f_gpu, f, equal_nan=True)
     st, t, _ = U.oracle_update(O, mesh, state, f, p, dt, 0.5, 0.05)
     assert st == 0 and t_gpu == t
-    assert np.array_equal(s_gpu, state)
+    assert np.array_equal(s_gpu[:5 + dim], state[:5 + dim], equal_nan=True)
 
 
 @pytest.mark.parametrize("dim", [2, 3])
