@@ -69,6 +69,7 @@ bool params_ok(const fvh_params *p, int dim) {
   return p && p->dim == dim && p->flux_kind >= 0 && p->flux_kind <= 2 &&
          p->limiter >= 0 && p->limiter <= 1 && (p->order == 1 || p->order == 2) &&
          (p->precision == FVH_PRECISION_FP64 || p->precision == FVH_PRECISION_MIXED) &&
+         (p->boundary == FVH_BOUNDARY_WALL || p->boundary == FVH_BOUNDARY_OUTFLOW) &&
          p->gamma > 1 && p->cv > 0 && p->cfl > 0;
 }
 

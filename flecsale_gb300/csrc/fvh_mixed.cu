@@ -426,8 +426,8 @@ template <int D, int KIND, bool SECOND>
 __global__ void __launch_bounds__(kCellThreads)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                    const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out, const double *dt,
-                   double factor, double gamma, double cv, int swap, double *soln_time,
-                   fvh_device_status *status) {
+                   double factor, double gamma, double cv, int swap, int outflow,
+                   double *soln_time, fvh_device_status *status) {
   // Reads only pk_in (all cells) and the cell's own FP64 state; writes the
   // cell's FP64 state and its pk_out record (null after the corrector).
   const double delta_t = dt[0] * factor;
@@ -459,6 +459,8 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     if (cc.y >= 0) {
       const prim<float, D> wr = recon<D, SECOND>(w, pk_in, cc.y, dx1, swap != 0);
       phys::riemann<float, D, KIND>(wl, wr, n, F);
+    } else if (outflow) {
+      phys::phys_flux<float, D>(wl, n, F);
     } else {
       phys::wall<float, D>(wl, n, F);
     }
@@ -593,7 +595,7 @@ static void launch_stage(workspace *w, const fvh_mesh_view &m, const fvh_params 
     mark("gradients");
   }
   flux_update_kernel<D, KIND, SECOND><<<nb, kCellThreads, 0, st>>>(
-      m, s, *w, pk_in, pk_out, dt, 0.5, p.gamma, p.cv, p.recon_swap_ep, t, status);
+      m, s, *w, pk_in, pk_out, dt, 0.5, p.gamma, p.cv, p.recon_swap_ep, p.boundary, t, status);
   mark("flux_update");
 }
 

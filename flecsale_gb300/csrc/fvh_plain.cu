@@ -376,7 +376,7 @@ __device__ __forceinline__ prim<D> reconstruct(const fvh_mesh_view &m,
 template <int D, int KIND, bool SECOND>
 __global__ void __launch_bounds__(kFaceThreads)
 fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
-              const fvh_flux_view fl, int swap) {
+              const fvh_flux_view fl, int swap, int outflow) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.num_faces) return;
   const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
@@ -396,6 +396,8 @@ fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_
       hllc<D>(wl, wr, n, F);
     else
       hlle<D>(wl, wr, n, F);
+  } else if (outflow) {
+    phys_flux<D>(wl, n, F);
   } else {
     F[0] = 0;
 #pragma unroll
@@ -496,11 +498,11 @@ static void launch_fluxes_kind(const fvh_mesh_view &m, const fvh_state_view &s,
                                const fvh_params &p, cudaStream_t st) {
   const int nb = (m.num_faces + kFaceThreads - 1) / kFaceThreads;
   if (p.flux_kind == FVH_FLUX_RUSANOV)
-    fluxes_kernel<D, FVH_FLUX_RUSANOV, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep);
+    fluxes_kernel<D, FVH_FLUX_RUSANOV, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
   else if (p.flux_kind == FVH_FLUX_HLLC)
-    fluxes_kernel<D, FVH_FLUX_HLLC, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep);
+    fluxes_kernel<D, FVH_FLUX_HLLC, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
   else
-    fluxes_kernel<D, FVH_FLUX_HLLE, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep);
+    fluxes_kernel<D, FVH_FLUX_HLLE, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
 }
 
 template <int D>

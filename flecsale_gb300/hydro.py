@@ -22,6 +22,7 @@ ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_OUT_OF_MEMORY, ERR_CAPACITY = 5, 6, 7, 8
 FLUX = {"hlle": 0, "rusanov": 1, "hllc": 2}
 LIMITER = {"barth_jespersen": 0, "none": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
+BOUNDARY = {"wall": 0, "outflow": 1}
 # fvh_problem_kind
 PROBLEM = {"shock_box": 0, "sod": 1, "four_quadrant": 2, "inner_cube": 3,
            "kelvin_helmholtz": 4, "uniform": 5}
@@ -34,7 +35,7 @@ _ip = C.POINTER(C.c_int32)
 class Params(C.Structure):
     _fields_ = [("dim", C.c_int32), ("flux_kind", C.c_int32), ("limiter", C.c_int32),
                 ("order", C.c_int32), ("recon_swap_ep", C.c_int32), ("precision", C.c_int32),
-                ("gamma", C.c_double), ("cv", C.c_double), ("cfl", C.c_double),
+                ("boundary", C.c_int32), ("reserved", C.c_int32), ("gamma", C.c_double), ("cv", C.c_double), ("cfl", C.c_double),
                 ("final_time", C.c_double)]
 
 
@@ -67,7 +68,7 @@ class FluxView(C.Structure):
 def make_params(dim: int, flux: str = "hlle", limiter: str = "barth_jespersen",
                 order: int = 2, swap: bool = True, precision: str = "fp64",
                 gamma: float = 1.4, cv: float = 1.0, cfl: Optional[float] = None,
-                final_time: float = 0.2) -> Params:
+                final_time: float = 0.2, boundary: str = "wall") -> Params:
     """fvh_params; defaults are the reference's (apps/hydro/2d/inputs.cc:27-42)."""
     p = Params()
     lib().fvh_params_default(C.byref(p), dim)
@@ -76,6 +77,7 @@ def make_params(dim: int, flux: str = "hlle", limiter: str = "barth_jespersen",
     p.order = order
     p.recon_swap_ep = 1 if swap else 0
     p.precision = PRECISION[precision]
+    p.boundary = BOUNDARY[boundary]
     p.gamma, p.cv = gamma, cv
     if cfl is not None:
         p.cfl = cfl

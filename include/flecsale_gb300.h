@@ -74,6 +74,14 @@ typedef enum fvh_limiter_kind {
   FVH_LIMITER_NONE = 1             /* unlimited least-squares gradients         */
 } fvh_limiter_kind;
 
+typedef enum fvh_boundary_kind {
+  FVH_BOUNDARY_WALL = 0,   /* reference: boundary_flux -> wall_flux,
+                              apps/hydro/types.h:132-137, euler_eqns.h:313-324 */
+  FVH_BOUNDARY_OUTFLOW = 1 /* not in the reference: transmissive boundary, the
+                              face flux is the physical flux of the reconstructed
+                              interior state, euler_eqns.h:274-304            */
+} fvh_boundary_kind;
+
 typedef enum fvh_precision {
   FVH_PRECISION_FP64 = 0,  /* everything in FP64 (reference arithmetic order)      */
   FVH_PRECISION_MIXED = 1  /* FP32 reconstruction + Riemann flux, FP64 state,
@@ -89,6 +97,8 @@ typedef struct fvh_params {
                              adds grad(e) to the face pressure and grad(p) to the
                              face energy (tasks.h:429-430, 448-449); 0 = textbook */
   int32_t precision;      /* fvh_precision                                        */
+  int32_t boundary;       /* fvh_boundary_kind for faces with one cell            */
+  int32_t reserved;       /* must be 0                                            */
   double gamma;           /* ideal gas ratio of specific heats (ideal_gas.h:42)   */
   double cv;              /* specific heat at constant volume                      */
   double cfl;             /* CFL number (inputs.h:64)                              */
@@ -96,7 +106,8 @@ typedef struct fvh_params {
 } fvh_params;
 
 /* Fill p with the reference's 2D shock-box defaults (apps/hydro/2d/inputs.cc:27-42):
- * HLLE, Barth-Jespersen, 2nd order, swap on, FP64, gamma 1.4, cv 1, CFL 0.5, t_f 0.2. */
+ * HLLE, Barth-Jespersen, 2nd order, swap on, FP64, walls, gamma 1.4, cv 1,
+ * CFL 0.5 (1/3 in 3D, 3d/inputs.cc:108), t_f 0.2. */
 void fvh_params_default(fvh_params *p, int32_t dim);
 
 /* ------------------------------------------------------------------------- */

@@ -372,6 +372,8 @@ void evaluate_fluxes(const fvh_mesh_view &m, const fvh_state_view &s,
         hllc<D>(wl, wr, n, F);
       else
         hlle<D>(wl, wr, n, F);
+    } else if (p.boundary == FVH_BOUNDARY_OUTFLOW) {
+      phys_flux<D>(wl, n, F);  // transmissive: ghost state = interior state
     } else {
       wall<D>(wl, n, F);
     }

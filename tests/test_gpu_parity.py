@@ -16,7 +16,10 @@ from tests import _util as U
 pytestmark = pytest.mark.gpu
 
 CASES = [
-    # dim, n, jitter, problem, flux, limiter, order, swap
+    # dim, n, jitter, problem, flux, limiter, order, swap[, boundary]
+    (2, (24, 17), 0.2, "four_quadrant", "hllc", "barth_jespersen", 2, True, "outflow"),
+    (2, (24, 17), 0.2, "four_quadrant", "rusanov", "barth_jespersen", 2, True, "outflow"),
+    (3, (7, 6, 5), 0.15, "inner_cube", "hllc", "barth_jespersen", 2, True, "outflow"),
     (2, (24, 17), 0.2, "four_quadrant", "hllc", "barth_jespersen", 2, True),
     (2, (24, 17), 0.2, "four_quadrant", "hlle", "barth_jespersen", 2, True),
     (2, (24, 17), 0.2, "kelvin_helmholtz", "rusanov", "barth_jespersen", 2, False),
@@ -31,9 +34,11 @@ CASES = [
 ]
 
 
-def _setup(cuda, dim, n, jitter, problem, flux, limiter, order, swap, warm_steps=2):
+def _setup(cuda, dim, n, jitter, problem, flux, limiter, order, swap, boundary="wall",
+           warm_steps=2):
     mesh = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, jitter, 7)
-    p = H.make_params(dim, flux=flux, limiter=limiter, order=order, swap=swap, cfl=0.4)
+    p = H.make_params(dim, flux=flux, limiter=limiter, order=order, swap=swap, cfl=0.4,
+                      boundary=boundary)
     state = H.initial_state(problem, mesh, p, seed=11)
     O = __import__("oracle").load()
     # advance a little on the oracle so gradients and limiters are active
@@ -42,7 +47,8 @@ def _setup(cuda, dim, n, jitter, problem, flux, limiter, order, swap, warm_steps
     return mesh, p, state, O
 
 
-@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}d-{c[3]}-{c[4]}-{c[5]}-o{c[6]}-s{int(c[7])}")
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}d-{c[3]}-{c[4]}-{c[5]}-o{c[6]}-s{int(c[7])}"
+                         + (f"-{c[8]}" if len(c) > 8 else ""))
 def test_tasks_bitwise(cuda, case):
     torch = cuda
     dim = case[0]
@@ -92,7 +98,7 @@ def test_tasks_bitwise(cuda, case):
 def test_solver_run_bitwise(cuda, dim):
     if dim == 2:
         mesh = H.HostMesh.box(2, (64, 48), [0, 0], [1, 1], 0.2, 1)
-        p = H.make_params(2, flux="hllc", cfl=0.4)
+        p = H.make_params(2, flux="hllc", cfl=0.4, boundary="outflow")
         state = H.initial_state("four_quadrant", mesh, p)
         nsteps = 30
     else:
@@ -234,7 +240,7 @@ def test_full_size_four_quadrant_bitwise_and_conservative(cuda):
     """1024^2 jittered four-quadrant (the benchmark workload), 2 steps: bitwise
     equal to the oracle; mass and energy conserved (walls only) to roundoff."""
     mesh = H.HostMesh.box(2, (1024, 1024), [0, 0], [1, 1], 0.2, 1)
-    p = H.make_params(2, flux="hllc", cfl=0.4)
+    p = H.make_params(2, flux="hllc", cfl=0.4)  # walls: mass and energy stay in the box
     state = H.initial_state("four_quadrant", mesh, p)
     vol = mesh.arrays()["cell_volume"]
     m0 = np.sum(state[0] * vol)
