@@ -174,7 +174,7 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (C++ restatement of the reference, OpenMP)
 # ---------------------------------------------------------------------------
-def cpu_baseline(mesh, params, state0, budget_s: float = 8.0, max_steps: int = 40) -> dict:
+def cpu_baseline(mesh, params, state0, budget_s: float = 12.0, max_steps: int = 400) -> dict:
     import oracle
     from tests import _util as U
     O = oracle.load()
