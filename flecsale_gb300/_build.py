@@ -33,6 +33,7 @@ UNITS = [
     ("fvh_plain.cu", ["--fmad=false"]),
     ("fvh_mixed.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("fvh_capi.cu", []),
+    ("fvh_noalloc.cu", []),
 ]
 
 

@@ -135,6 +135,9 @@ def _declare(L: C.CDLL) -> None:
         "fvh_solver_advance_host": (C.c_int, [vp, C.POINTER(StateView), _dp, C.c_int64,
                                               C.POINTER(C.c_double), vp]),
         "fvh_solver_launches_per_step": (C.c_int32, [vp]),
+        "fvh_evaluate_time_step_noalloc": (C.c_int, [C.POINTER(MeshView), C.POINTER(StateView),
+                                                     C.POINTER(Params), vp, vp, vp, vp]),
+        "fvh_time_step_noalloc_max_cells": (C.c_int32, []),
         "fvh_solver_profile": (C.c_int, [vp, C.POINTER(StateView), C.c_int32, C.c_int32,
                                          C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), vp]),

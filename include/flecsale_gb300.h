@@ -196,6 +196,25 @@ fvh_status fvh_evaluate_time_step(const fvh_mesh_view *mesh,
                                   fvh_device_status *d_status,
                                   fvh_stream_t stream);
 
+/* No counterpart in the reference.  Same result as fvh_evaluate_time_step, for
+ * callers that cannot allocate device memory (a task runtime that owns all
+ * device memory and hands a task only its field buffers, or a hot loop that
+ * must not pay cudaMalloc's implicit synchronisation).  It takes no workspace:
+ * the partial maxima live in a 64 KiB array inside the library, which every
+ * GPU that loads the library holds until exit.  Meshes with more than
+ * fvh_time_step_noalloc_max_cells() = 2,097,152 cells are rejected with
+ * FVH_ERR_CAPACITY.  The first call on a device looks up that array's device
+ * address (make it before any stream capture).  All calls share the array:
+ * calls whose kernels overlap on the GPU (e.g. on two streams) race.  It calls
+ * no cudaMalloc, cudaFree or allocating routine. */
+fvh_status fvh_evaluate_time_step_noalloc(const fvh_mesh_view *mesh,
+                                          const fvh_state_view *state,
+                                          const fvh_params *params,
+                                          const double *d_soln_time, double *d_dt,
+                                          fvh_device_status *d_status,
+                                          fvh_stream_t stream);
+int32_t fvh_time_step_noalloc_max_cells(void);
+
 /* Replaces evaluate_gradients (tasks.h:145-321): vertex-neighbour least squares
  * gradients of (d, v, e, p, a) with the Barth-Jespersen vertex limiter. */
 fvh_status fvh_evaluate_gradients(const fvh_mesh_view *mesh,
