@@ -45,9 +45,9 @@ WORKLOAD = ("2D four-quadrant Riemann problem, 1024x1024 quads on [0,1]^2 jitter
             "HLLC, transmissive boundaries, CFL 0.4, one step = dt + predictor + corrector")
 
 
-def build_problem():
+def build_problem(n_side: int = N_SIDE):
     import flecsale_gb300.hydro as H
-    mesh = H.HostMesh.box(2, (N_SIDE, N_SIDE), [0, 0], [1, 1], JITTER, SEED)
+    mesh = H.HostMesh.box(2, (n_side, n_side), [0, 0], [1, 1], JITTER, SEED)
     kw = dict(flux="hllc", limiter="barth_jespersen", order=2, swap=True, cfl=0.4,
               final_time=1.0e9, boundary="outflow")
     p64 = H.make_params(2, precision="fp64", **kw)
@@ -208,7 +208,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    H, mesh, p64, _, state0 = build_problem()
+    H, mesh, p64, _, state0 = build_problem(args.n)
     import oracle
     from tests import _util as U
     O = oracle.load()
@@ -235,6 +235,57 @@ def run_reference(args):
     return 0
 
 
+BATCH_PROBLEMS, BATCH_SEED = 512, 3
+BATCH_KINDS = ("kelvin_helmholtz", "four_quadrant", "sod")
+
+
+def batch_problems(n=BATCH_PROBLEMS, seed=BATCH_SEED):
+    """Sizes log-uniform in [32^2, 512^2] cells (side log-uniform in [32, 512]),
+    jitter +-0.2h, problem kinds cycling KH shear layer / four-quadrant / Sod."""
+    import flecsale_gb300.hydro as H
+    rng = np.random.default_rng(seed)
+    sides = np.exp(rng.uniform(np.log(32), np.log(512), n)).round().astype(int)
+    return [(H.HostMesh.box(2, (int(s), int(s)), [0, 0], [1, 1], JITTER, 1000 + k),
+             BATCH_KINDS[k % 3]) for k, s in enumerate(sides)]
+
+
+def run_batched(torch, stream, steps: int, warmup: int) -> dict:
+    """The batched form: all problems advanced by one CUDA-graph launch per
+    step, per-problem dt, launch shape picked by the autotuner."""
+    import flecsale_gb300.hydro as H
+    t0 = time.perf_counter()
+    probs = batch_problems()
+    p = H.make_params(2, flux="hllc", precision="mixed", boundary="outflow", cfl=0.4,
+                      final_time=1.0e9)
+    meshes = [m for m, _ in probs]
+    b = H.Batch.for_meshes(p, meshes)
+    b.assign(meshes, 0.4, 1.0e9, stream=stream)
+    for k, (m, kind) in enumerate(probs):
+        b.set_state(k, H.initial_state(kind, m, p, seed=k), 0.0, stream)
+    setup_s = time.perf_counter() - t0
+    tune = b.autotune(trial_steps=3, use_cache=False, stream=stream)
+    for _ in range(warmup):
+        b.step(1, stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(steps, stream)  # one graph launch advances every problem `steps` steps
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    _, codes, _ = b.query(stream)
+    if np.any(codes != 0):
+        raise RuntimeError(f"batched: device status {codes[codes != 0][:4]}")
+    nc = b.num_cells
+    return {"value": nc * steps / (ms * 1e-3), "unit": UNIT, "problems": len(meshes),
+            "cells": nc, "steps": steps, "ms_per_step": ms / steps,
+            "launches": "one CUDA graph launch for all steps",
+            "gpu_launches": b.launches_per_step() * steps,
+            "autotuned_shape": tune, "host_setup_s": setup_s,
+            "config": "512 independent 2D problems, cells log-uniform in [32^2, 512^2] (seed 3), "
+                      "KH shear layer / four-quadrant / Sod, HLLC, outflow, CFL 0.4, mixed precision"}
+
+
 def timed_steps(torch, solver, dstate, stream, K, dist):
     if dist:
         dist.barrier()
@@ -258,7 +309,7 @@ def run_ours(args):
     import torch
     dist, ws, rank, local = dist_setup("nccl")
     torch.cuda.set_device(local)
-    H, mesh, p64, p32, state0 = build_problem()
+    H, mesh, p64, p32, state0 = build_problem(args.n)
     stream = torch.cuda.Stream()
     dmesh = H.DeviceMesh(mesh)
     nc = mesh.num_cells
@@ -366,6 +417,9 @@ def run_ours(args):
                      "l1_total_energy_mixed_vs_fp64": l1(E(m), E(f)),
                      "linf_density_mixed_vs_fp64": float(np.abs(m[0] - f[0]).max())},
     }
+    if not args.no_batch:
+        line["batched"] = run_batched(torch, stream, min(args.steps, 50), args.warmup)
+        line["batched_over_fp64"] = line["batched"]["value"] / line["plain_fp64"]["value"]
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mesh, p64, state0)
     print(json.dumps(line), flush=True)
@@ -381,6 +435,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batched form")
+    ap.add_argument("--n", type=int, default=N_SIDE, help="mesh side (default 1024)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

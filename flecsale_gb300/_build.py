@@ -34,6 +34,7 @@ UNITS = [
     ("fvh_mixed.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("fvh_capi.cu", []),
     ("fvh_noalloc.cu", []),
+    ("fvh_batch.cu", []),
 ]
 
 

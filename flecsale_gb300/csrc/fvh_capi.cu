@@ -89,6 +89,8 @@ struct fvh_solver {
   fvh_gradient_view grads{};
   fvh_flux_view flux{};
   double *work = nullptr;          // gradients + fluxes
+  double *tables = nullptr;        // FP64 path: per-cell LSQ matrices, per-slot V/A
+  double *lsq = nullptr, *slot_dx = nullptr;
   double *scalars = nullptr;       // [0] soln time, [1] dt, [2..] dt partials
   fvh_device_status *status = nullptr;
   double *host_scalars = nullptr;  // pinned: soln time
@@ -237,6 +239,7 @@ void fvh_solver_destroy(fvh_solver *s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->mixed) fvh::mixed::destroy(s->mixed);
   cudaFree(s->work);
+  cudaFree(s->tables);
   cudaFree(s->scalars);
   cudaFree(s->status);
   cudaFreeHost(s->host_scalars);
@@ -271,6 +274,18 @@ fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params
       for (int i = 0; i < D; ++i, b += nf) s->flux.momentum[i] = b;
       s->flux.energy = b;
     }
+    // geometry-only tables (built once, same arithmetic as on the fly)
+    int32_t nnz = 0;
+    if (e == cudaSuccess)
+      e = cudaMemcpy(&nnz, mesh->cell_face_offsets + nc, sizeof(int32_t), cudaMemcpyDeviceToHost);
+    const size_t nlsq = (size_t)fvh::plain::lsq_doubles_per_cell(D) * nc;
+    if (e == cudaSuccess) e = cudaMalloc(&s->tables, sizeof(double) * (nlsq + (size_t)nnz + 1));
+    if (e == cudaSuccess) {
+      s->lsq = s->tables;
+      s->slot_dx = s->tables + nlsq;
+      e = D == 2 ? fvh::plain::build_tables<2>(*mesh, s->lsq, s->slot_dx)
+                 : fvh::plain::build_tables<3>(*mesh, s->lsq, s->slot_dx);
+    }
   } else {
     const fvh_status ms = fvh::mixed::create(*mesh, *params, &s->mixed);
     if (ms != FVH_OK) {
@@ -303,12 +318,19 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   if (p.precision == FVH_PRECISION_MIXED)
     return from_cuda(fvh::mixed::step(s->mixed, m, p, *state, t, dt, partial,
                                       dt_blocks(m.num_cells), s->status, st, mark));
-  const size_t wsb = fvh_time_step_workspace_bytes(m.num_cells);
   const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
-  fvh_status r = fvh_evaluate_time_step(&m, state, &p, t, dt, partial, wsb, s->status, fs);
+  const int nb = dt_blocks(m.num_cells);
+  fvh_status r = from_cuda(
+      m.dim == 2 ? fvh::plain::launch_dt<2>(m, *state, p, t, dt, partial, nb, s->status, st, s->slot_dx)
+                 : fvh::plain::launch_dt<3>(m, *state, p, t, dt, partial, nb, s->status, st, s->slot_dx));
   mark("dt");
   for (int stage = 0; stage < 2 && r == FVH_OK; ++stage) {
-    r = fvh_evaluate_gradients(&m, state, &s->grads, &p, fs);
+    if (p.order == 1)
+      r = fvh_evaluate_gradients(&m, state, &s->grads, &p, fs);
+    else
+      r = from_cuda(m.dim == 2
+                        ? fvh::plain::launch_gradients<2>(m, *state, s->grads, p, st, s->lsq)
+                        : fvh::plain::launch_gradients<3>(m, *state, s->grads, p, st, s->lsq));
     mark("gradients");
     if (r == FVH_OK) r = fvh_evaluate_fluxes(&m, state, &s->grads, &s->flux, &p, fs);
     mark("fluxes");

@@ -45,15 +45,20 @@ __device__ inline double block_max(double v) {
 #endif
 
 namespace plain {
+// slot_dx / lsq: optional per-mesh tables (null = compute on the fly; the
+// results are the same either way)
 template <int D>
 cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
                       const fvh_params &p, const double *soln_time, double *dt,
                       double *partial, int nblocks, fvh_device_status *status,
-                      cudaStream_t st);
+                      cudaStream_t st, const double *slot_dx = nullptr);
 template <int D>
 cudaError_t launch_gradients(const fvh_mesh_view &m, const fvh_state_view &s,
                              const fvh_gradient_view &g, const fvh_params &p,
-                             cudaStream_t st);
+                             cudaStream_t st, const double *lsq = nullptr);
+template <int D>
+cudaError_t build_tables(const fvh_mesh_view &m, double *lsq, double *slot_dx);
+int lsq_doubles_per_cell(int dim);
 template <int D>
 cudaError_t launch_fluxes(const fvh_mesh_view &m, const fvh_state_view &s,
                           const fvh_gradient_view &g, const fvh_flux_view &fl,

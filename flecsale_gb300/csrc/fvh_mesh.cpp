@@ -486,6 +486,59 @@ fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
 
 void fvh_host_mesh_destroy(fvh_host_mesh *m) { delete m; }
 
+fvh_status fvh_host_mesh_concat(int32_t n, const fvh_host_mesh *const *meshes,
+                                fvh_host_mesh **out) {
+  if (!out || n <= 0 || !meshes) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const int dim = meshes[0] ? meshes[0]->dim : 0;
+  int64_t nc = 0, nf = 0, nv = 0, ncf = 0, nnb = 0, ncv = 0, nfv = 0;
+  for (int k = 0; k < n; ++k) {
+    const fvh_host_mesh *m = meshes[k];
+    if (!m || m->dim != dim) return FVH_ERR_INVALID_ARGUMENT;
+    nc += m->nc; nf += m->nf; nv += m->nv;
+    ncf += m->cf.size(); nnb += m->nb.size(); ncv += m->cv.size(); nfv += m->fv.size();
+  }
+  if (nc >= INT32_MAX || nf >= INT32_MAX || nv >= INT32_MAX || ncf >= INT32_MAX ||
+      nnb >= INT32_MAX || ncv >= INT32_MAX || nfv >= INT32_MAX)
+    return FVH_ERR_CAPACITY;
+  fvh_host_mesh *o = new (std::nothrow) fvh_host_mesh();
+  if (!o) return FVH_ERR_OUT_OF_MEMORY;
+  o->dim = dim;
+  o->nc = (int)nc; o->nf = (int)nf; o->nv = (int)nv;
+  o->cf_off.assign(1, 0); o->nb_off.assign(1, 0); o->cv_off.assign(1, 0); o->fv_off.assign(1, 0);
+  int32_t co = 0, fo = 0, vo = 0;
+  for (int k = 0; k < n; ++k) {
+    const fvh_host_mesh &m = *meshes[k];
+    for (int f = 0; f < m.nf; ++f) {
+      const int32_t a = m.face_cells[2 * (size_t)f], b = m.face_cells[2 * (size_t)f + 1];
+      o->face_cells.push_back(a + co);
+      o->face_cells.push_back(b < 0 ? -1 : b + co);
+    }
+    auto append_csr = [](std::vector<int32_t> &off, std::vector<int32_t> &dst,
+                         const std::vector<int32_t> &soff, const std::vector<int32_t> &src,
+                         auto shift) {
+      const int32_t base = off.back();
+      for (size_t i = 1; i < soff.size(); ++i) off.push_back(base + soff[i]);
+      for (int32_t x : src) dst.push_back(shift(x));
+    };
+    append_csr(o->cf_off, o->cf, m.cf_off, m.cf, [fo](int32_t f) { return f >= 0 ? f + fo : ~(~f + fo); });
+    append_csr(o->nb_off, o->nb, m.nb_off, m.nb, [co](int32_t c) { return c + co; });
+    append_csr(o->cv_off, o->cv, m.cv_off, m.cv, [vo](int32_t v) { return v + vo; });
+    append_csr(o->fv_off, o->fv, m.fv_off, m.fv, [vo](int32_t v) { return v + vo; });
+    for (int d = 0; d < 3; ++d) {
+      o->cc[d].insert(o->cc[d].end(), m.cc[d].begin(), m.cc[d].end());
+      o->fc[d].insert(o->fc[d].end(), m.fc[d].begin(), m.fc[d].end());
+      o->fn[d].insert(o->fn[d].end(), m.fn[d].begin(), m.fn[d].end());
+      o->vc[d].insert(o->vc[d].end(), m.vc[d].begin(), m.vc[d].end());
+    }
+    o->cvol.insert(o->cvol.end(), m.cvol.begin(), m.cvol.end());
+    o->fa.insert(o->fa.end(), m.fa.begin(), m.fa.end());
+    co += m.nc; fo += m.nf; vo += m.nv;
+  }
+  *out = o;
+  return FVH_OK;
+}
+
 fvh_status fvh_host_mesh_view(const fvh_host_mesh *m, fvh_mesh_view *o) {
   if (!m || !o) return FVH_ERR_INVALID_ARGUMENT;
   std::memset(o, 0, sizeof(*o));

@@ -45,6 +45,7 @@ struct layout {
   static constexpr int CEN4 = D == 2 ? 1 : 2;  // centroid hi/lo
   static constexpr int FGEO4 = 1;              // normal[D], area
   static constexpr int FDX4 = D == 2 ? 1 : 2;  // x_f - x_c0, x_f - x_c1
+  static constexpr int FLUX4 = D == 2 ? 1 : 2; // face flux (D+2 floats, padded)
 };
 
 struct workspace {
@@ -57,7 +58,9 @@ struct workspace {
   float4 *vcoord = nullptr;  // vertex coordinates hi/lo
   float4 *fgeo = nullptr;    // face normal + area
   float4 *fdx = nullptr;     // face centroid offsets from both cells
+  float4 *fflux = nullptr;   // face schedule: area-scaled face fluxes
   double *inv_vol = nullptr; // 1/V (FP64)
+  float *inv_vol32 = nullptr; // 1/V (FP32, for the CFL estimate)
 };
 
 // Load pack fields: slots (d, v0, v1, [v2,] p, e, a) in the AoS order
@@ -126,6 +129,42 @@ __device__ __forceinline__ float2 split(double x) {
   return make_float2(h, (float)(x - (double)h));
 }
 
+// FP32 <-> FP64 conversions done with integer instructions, so they do not
+// occupy the (narrow) FP64 pipe.  Values in the FP32 subnormal range flush to
+// a signed zero; infinities and NaNs keep their class.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned sign = u & 0x80000000u;
+  const unsigned ed = e == 0xffu ? 0x7ffu : e + 896u;
+  const unsigned hi = e == 0 ? sign : (sign | (ed << 20) | ((u & 0x7fffffu) >> 3));
+  const unsigned lo = e == 0 ? 0u : (u << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// round to nearest even
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // FP32 biased exponent
+  unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned r = lo & 0x1fffffffu;
+  const unsigned up = (r > 0x10000000u) | ((r == 0x10000000u) & (m & 1u));
+  unsigned f = (((unsigned)e) << 23) + m + up;  // a carry out of m bumps the exponent
+  f = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : f);
+  return __uint_as_float(sign | f);
+}
+
+// error-free sum s + x -> (s', err) (Knuth's two-sum).  The _rn intrinsics
+// are never contracted into FMAs, which would break the identity.
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
 // ---------------------------------------------------------------------------
 // setup: FP32 geometry derived once from the FP64 mesh
 // ---------------------------------------------------------------------------
@@ -147,6 +186,7 @@ __global__ void setup_cells(const fvh_mesh_view m, workspace w) {
     w.ccen[2 * (size_t)c + 1] = make_float4(lo[0], lo[1], lo[D - 1], 0.f);
   }
   w.inv_vol[c] = 1.0 / m.cell_volume[c];
+  w.inv_vol32[c] = (float)(1.0 / m.cell_volume[c]);
 }
 
 template <int D>
@@ -205,6 +245,22 @@ __device__ __forceinline__ void face_geo(const workspace &w, int f, float *n, fl
   }
 }
 
+// block-wide FP32 maximum (valid in thread 0); all threads must call it
+__device__ __forceinline__ float block_max_f(float v) {
+  __shared__ float warp_max[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_max[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < (int)((blockDim.x + 31) >> 5) ? warp_max[lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // pack + dt partial maxima
 // ---------------------------------------------------------------------------
@@ -217,11 +273,11 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
        c += gridDim.x * blockDim.x) {
     float v[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i) v[i] = (float)s.velocity[i][c];
-    const float a = (float)s.sound_speed[c];
-    store_pack<D>(w.pack, c, (float)s.density[c], v, (float)s.pressure[c],
-                  (float)s.internal_energy[c], a);
-    const float iv = (float)w.inv_vol[c];
+    for (int i = 0; i < D; ++i) v[i] = d2f(s.velocity[i][c]);
+    const float a = d2f(s.sound_speed[c]);
+    store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
+                  d2f(s.internal_energy[c]), a);
+    const float iv = w.inv_vol32[c];
     const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
     for (int q = q0; q < q1; ++q) {
       int f = m.cell_faces[q];
@@ -232,8 +288,8 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
       dt_inv = smax(dti, dt_inv);
     }
   }
-  const double m_ = block_max((double)dt_inv);
-  if (threadIdx.x == 0) partial[blockIdx.x] = m_;
+  dt_inv = block_max_f(dt_inv);
+  if (threadIdx.x == 0) partial[blockIdx.x] = f2d(dt_inv);
 }
 
 __global__ void __launch_bounds__(kDtThreads)
@@ -255,16 +311,94 @@ dt_final_kernel(const double *partial, int nblocks, fvh_params p, const double *
   }
 }
 
+// Batch form: per-problem maxima.  A block (or warp) whose cells all belong to
+// one problem reduces first and issues one integer atomicMax on the FP32 bits
+// (non-negative floats order like their bit patterns), so the result does not
+// depend on the order of the atomics.
+template <int D>
+__global__ void __launch_bounds__(kDtThreads)
+pack_dt_batch_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
+                     const problem_map pm) {
+  __shared__ int block_pr[kDtThreads / 32];
+  __shared__ float block_v[kDtThreads / 32];
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  float dti_c = 0.f;
+  int pr = -1;
+  if (c < m.num_cells) {
+    pr = pm.cell_problem[c];
+    float v[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) v[i] = d2f(s.velocity[i][c]);
+    const float a = d2f(s.sound_speed[c]);
+    store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
+                  d2f(s.internal_energy[c]), a);
+    const float iv = w.inv_vol32[c];
+    for (int q = m.cell_face_offsets[c]; q < m.cell_face_offsets[c + 1]; ++q) {
+      int f = m.cell_faces[q];
+      f = f < 0 ? ~f : f;
+      float n[D], area;
+      face_geo<D>(w, f, n, area);
+      dti_c = smax((a + fabsf(phys::dot<float, D>(v, n))) * (area * iv), dti_c);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int pr0 = __shfl_sync(0xffffffffu, pr, 0);
+  const bool warp_uniform = __all_sync(0xffffffffu, pr == pr0);
+  float wm = dti_c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+  if (lane == 0) {
+    block_pr[warp] = warp_uniform ? pr0 : -2;
+    block_v[warp] = wm;
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  bool block_uniform = true;
+  for (int k = 0; k < nw; ++k) block_uniform = block_uniform && block_pr[k] == block_pr[0];
+  if (block_uniform) {
+    if (threadIdx.x == 0 && block_pr[0] >= 0) {
+      float bm = 0.f;
+      for (int k = 0; k < nw; ++k) bm = fmaxf(bm, block_v[k]);
+      atomicMax(&pm.dtinv_bits[block_pr[0]], __float_as_uint(bm));
+    }
+  } else if (warp_uniform) {
+    if (lane == 0 && pr0 >= 0) atomicMax(&pm.dtinv_bits[pr0], __float_as_uint(wm));
+  } else if (pr >= 0) {
+    atomicMax(&pm.dtinv_bits[pr], __float_as_uint(dti_c));
+  }
+}
+
+// dt per problem; resets the accumulator for the next step.  A problem that
+// has reached its final time gets dt = 0 and no longer changes.
+__global__ void dt_final_batch_kernel(const problem_map pm, fvh_device_status dummy) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= pm.nproblems) return;
+  const double dt_inv = f2d(__uint_as_float(pm.dtinv_bits[k]));
+  pm.dtinv_bits[k] = 0u;
+  const double max_dt = pm.final_time[k] - pm.t[k];
+  if (pm.t[k] >= pm.final_time[k] - 1e-12 * fabs(pm.final_time[k])) {
+    pm.dt[k] = 0;  // finished (the last clamped step can land an ulp short)
+  } else if (dt_inv <= 0) {
+    atomicMin(&pm.status[k], status_key(0, FVH_ERR_INFINITE_DT));
+    pm.dt[k] = 0;
+  } else {
+    double time_step = 1 / dt_inv;
+    time_step *= pm.cfl[k];
+    time_step = smin(time_step, max_dt);
+    pm.dt[k] = time_step > 0 ? time_step : 0.0;
+  }
+  (void)dummy;
+}
+
 // ---------------------------------------------------------------------------
 // FP32 gradients + Barth-Jespersen vertex limiter
 // ---------------------------------------------------------------------------
-template <int D, bool LIMIT>
-__global__ void __launch_bounds__(kCellThreads)
+template <int D, bool LIMIT, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS)
 gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk) {
   constexpr int NV = D + 4;
   constexpr float tol = 1.e-9f;
-  const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c0 >= m.num_cells) return;
+  for (int c0 = blockIdx.x * BS + threadIdx.x; c0 < m.num_cells; c0 += gridDim.x * BS) {
   float xh[3], xl[3];
   load_cen<D>(w.ccen, c0, xh, xl);
   float u0[NV], umin[NV], umax[NV];
@@ -287,6 +421,7 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 #pragma unroll
     for (int j = 0; j < D; ++j) b[k][j] = 0.f;
   const int q0 = m.cell_nbr_offsets[c0], q1 = m.cell_nbr_offsets[c0 + 1];
+#pragma unroll 4
   for (int q = q0; q < q1; ++q) {
     const int c1 = m.cell_nbrs[q];
     const prim<float, D> p = load_pack<D>(pk, c1);
@@ -393,6 +528,7 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
   for (int q = 0; q < G4; ++q)
     w.grads[(size_t)G4 * c0 + q] =
         make_float4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
+  }  // cells
 }
 
 // ---------------------------------------------------------------------------
@@ -422,56 +558,50 @@ __device__ __forceinline__ prim<float, D> recon(const workspace &w, const float4
   return u;
 }
 
+// Area-scaled flux of face f in its own orientation (cells(f)[0] -> [1]),
+// F[k] = RN(flux_k * A_f).  Both cells of a face and the face kernel get the
+// same bits from it.
 template <int D, int KIND, bool SECOND>
-__global__ void __launch_bounds__(kCellThreads)
-flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
-                   const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out, const double *dt,
-                   double factor, double gamma, double cv, int swap, int outflow,
-                   double *soln_time, fvh_device_status *status) {
-  // Reads only pk_in (all cells) and the cell's own FP64 state; writes the
-  // cell's FP64 state and its pk_out record (null after the corrector).
-  const double delta_t = dt[0] * factor;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c == 0) soln_time[0] = soln_time[0] + delta_t;
-  if (c >= m.num_cells) return;
+__device__ __forceinline__ void face_flux_area(const fvh_mesh_view &m, const workspace &w,
+                                               const float4 *__restrict__ pk, int f, int swap,
+                                               int outflow, float *F) {
+  const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
+  float n[D], area;
+  face_geo<D>(w, f, n, area);
+  float dx0[D], dx1[D];
+  if (D == 2) {
+    const float4 t = w.fdx[f];
+    dx0[0] = t.x; dx0[1] = t.y; dx1[0] = t.z; dx1[1] = t.w;
+  } else {
+    const float4 a = w.fdx[2 * (size_t)f], b = w.fdx[2 * (size_t)f + 1];
+    dx0[0] = a.x; dx0[1] = a.y; dx0[D - 1] = a.z;
+    dx1[0] = b.x; dx1[1] = b.y; dx1[D - 1] = b.z;
+  }
+  const prim<float, D> wl = recon<D, SECOND>(w, pk, cc.x, dx0, swap != 0);
+  if (cc.y >= 0) {
+    const prim<float, D> wr = recon<D, SECOND>(w, pk, cc.y, dx1, swap != 0);
+    phys::riemann<float, D, KIND>(wl, wr, n, F);
+  } else if (outflow) {
+    phys::phys_flux<float, D>(wl, n, F);
+  } else {
+    phys::wall<float, D>(wl, n, F);
+  }
+#pragma unroll
+  for (int k = 0; k < D + 2; ++k) F[k] = __fmul_rn(F[k], area);
+}
+
+// Conservative FP64 update of cell c from its compensated face sums
+// (update_state_from_flux + update_state_from_energy), writes the FP64 state
+// and the next pack record.
+template <int D>
+__device__ __forceinline__ void cell_update(const fvh_state_view &s, const workspace &w,
+                                            float4 *__restrict__ pk_out, const problem_map &pm,
+                                            int c, int pr, double delta_t, const float *shi,
+                                            const float *slo, double gm1, float ggm1,
+                                            double inv_cv) {
   double du[D + 2];
 #pragma unroll
-  for (int k = 0; k < D + 2; ++k) du[k] = 0.0;
-  const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
-  for (int q = q0; q < q1; ++q) {
-    const int sf = m.cell_faces[q];
-    const int f = sf < 0 ? ~sf : sf;
-    const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
-    float n[D], area;
-    face_geo<D>(w, f, n, area);
-    float dx0[D], dx1[D];
-    if (D == 2) {
-      const float4 t = w.fdx[f];
-      dx0[0] = t.x; dx0[1] = t.y; dx1[0] = t.z; dx1[1] = t.w;
-    } else {
-      const float4 a = w.fdx[2 * (size_t)f], b = w.fdx[2 * (size_t)f + 1];
-      dx0[0] = a.x; dx0[1] = a.y; dx0[D - 1] = a.z;
-      dx1[0] = b.x; dx1[1] = b.y; dx1[D - 1] = b.z;
-    }
-    // always evaluated in the face's own orientation (cells(f)[0] -> [1])
-    const prim<float, D> wl = recon<D, SECOND>(w, pk_in, cc.x, dx0, swap != 0);
-    float F[D + 2];
-    if (cc.y >= 0) {
-      const prim<float, D> wr = recon<D, SECOND>(w, pk_in, cc.y, dx1, swap != 0);
-      phys::riemann<float, D, KIND>(wl, wr, n, F);
-    } else if (outflow) {
-      phys::phys_flux<float, D>(wl, n, F);
-    } else {
-      phys::wall<float, D>(wl, n, F);
-    }
-    if (sf >= 0) {
-#pragma unroll
-      for (int k = 0; k < D + 2; ++k) du[k] -= (double)(F[k] * area);
-    } else {
-#pragma unroll
-      for (int k = 0; k < D + 2; ++k) du[k] += (double)(F[k] * area);
-    }
-  }
+  for (int k = 0; k < D + 2; ++k) du[k] = f2d(shi[k]) + f2d(slo[k]);
   const double scale = delta_t * w.inv_vol[c];
   double vel[D];
 #pragma unroll
@@ -483,7 +613,7 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
   for (int i = 0; i < D; ++i) ke += vel[i] * vel[i];
   const double ener = den0 * (s.internal_energy[c] + 0.5 * ke) + du[D + 1] * scale;
   // 1/mass: FP32 estimate refined by one Newton step in FP64
-  double inv_mass = (double)(1.0f / (float)mass);
+  double inv_mass = f2d(__frcp_rn(d2f(mass)));
   inv_mass = inv_mass * (2.0 - mass * inv_mass);
   ke = 0.0;
 #pragma unroll
@@ -492,22 +622,105 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     ke += vel[i] * vel[i];
   }
   const double e = ener * inv_mass - 0.5 * ke;
-  const double p = (gamma - 1.0) * mass * e;
-  const float a = sqrtf((float)(gamma * (gamma - 1.0)) * (float)e);
+  const double p = gm1 * mass * e;
+  const float ef = d2f(e);
+  const float a = sqrtf(ggm1 * ef);
   s.density[c] = mass;
 #pragma unroll
   for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
   s.internal_energy[c] = e;
   s.pressure[c] = p;
-  s.temperature[c] = e * (1.0 / cv);
-  s.sound_speed[c] = (double)a;
+  s.temperature[c] = e * inv_cv;
+  s.sound_speed[c] = f2d(a);
   if (pk_out) {
     float vf[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i) vf[i] = (float)vel[i];
-    store_pack<D>(pk_out, c, (float)mass, vf, (float)p, (float)e, a);
+    for (int i = 0; i < D; ++i) vf[i] = d2f(vel[i]);
+    store_pack<D>(pk_out, c, d2f(mass), vf, d2f(p), ef, a);
   }
-  if (e < 0 || mass < 0) atomicMin(status, status_key(c, FVH_ERR_NEGATIVE_STATE));
+  if (e < 0 || mass < 0) atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
+}
+
+// Cell-centric schedule: each cell evaluates the fluxes of its own faces.
+template <int D, int KIND, bool SECOND, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS)
+flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
+                   const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out,
+                   const problem_map pm, double factor, double gm1, float ggm1, double inv_cv,
+                   int swap, int outflow) {
+  // Reads only pk_in (all cells) and the cell's own FP64 state; writes the
+  // cell's FP64 state and its pk_out record (null after the corrector).
+  for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
+    const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
+    const double delta_t = pm.dt[pr] * factor;
+    if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
+    // face sums in FP32 with error-free two-sum compensation (hi + lo carries
+    // about 48 bits), one FP64 add per component afterwards
+    float shi[D + 2], slo[D + 2];
+#pragma unroll
+    for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
+    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
+#pragma unroll 2
+    for (int q = q0; q < q1; ++q) {
+      const int sf = m.cell_faces[q];
+      float F[D + 2];
+      face_flux_area<D, KIND, SECOND>(m, w, pk_in, sf < 0 ? ~sf : sf, swap, outflow, F);
+#pragma unroll
+      for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
+    }
+    cell_update<D>(s, w, pk_out, pm, c, pr, delta_t, shi, slo, gm1, ggm1, inv_cv);
+  }
+}
+
+// Face schedule, part 1: one flux per face into the FP32 face-flux array.
+template <int D, int KIND, bool SECOND, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS)
+face_flux_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk_in, int swap,
+                 int outflow) {
+  constexpr int F4 = layout<D>::FLUX4;
+  for (int f = blockIdx.x * BS + threadIdx.x; f < m.num_faces; f += gridDim.x * BS) {
+    float F[4 * F4];
+    face_flux_area<D, KIND, SECOND>(m, w, pk_in, f, swap, outflow, F);
+#pragma unroll
+    for (int k = D + 2; k < 4 * F4; ++k) F[k] = 0.f;
+#pragma unroll
+    for (int q = 0; q < F4; ++q)
+      w.fflux[(size_t)F4 * f + q] = make_float4(F[4 * q], F[4 * q + 1], F[4 * q + 2], F[4 * q + 3]);
+  }
+}
+
+// Face schedule, part 2: cell-centric gather of the face-flux array + update.
+template <int D, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS)
+gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
+                     float4 *__restrict__ pk_out, const problem_map pm, double factor,
+                     double gm1, float ggm1, double inv_cv) {
+  constexpr int F4 = layout<D>::FLUX4;
+  for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
+    const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
+    const double delta_t = pm.dt[pr] * factor;
+    if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
+    float shi[D + 2], slo[D + 2];
+#pragma unroll
+    for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
+    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
+    for (int q = q0; q < q1; ++q) {
+      const int sf = m.cell_faces[q];
+      const int f = sf < 0 ? ~sf : sf;
+      float F[4 * F4];
+#pragma unroll
+      for (int r = 0; r < F4; ++r) {
+        const float4 t = w.fflux[(size_t)F4 * f + r];
+        F[4 * r] = t.x;
+        F[4 * r + 1] = t.y;
+        F[4 * r + 2] = t.z;
+        F[4 * r + 3] = t.w;
+      }
+#pragma unroll
+      for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
+    }
+    cell_update<D>(s, w, pk_out, pm, c, pr, delta_t, shi, slo, gm1, ggm1, inv_cv);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -517,8 +730,8 @@ template <int D>
 static size_t bytes_for(int nc, int nf, int nv) {
   using L = layout<D>;
   return sizeof(float4) * ((size_t)nc * (2 * L::PACK4 + L::GRAD4 + L::CEN4) + (size_t)nv * L::CEN4 +
-                           (size_t)nf * (L::FGEO4 + L::FDX4)) +
-         sizeof(double) * (size_t)nc + 256 * 8;
+                           (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4)) +
+         sizeof(double) * (size_t)nc + sizeof(float) * (size_t)nc + 256 * 9;
 }
 
 template <int D>
@@ -537,40 +750,64 @@ static void carve(workspace *w) {
   w->vcoord = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nv * L::CEN4));
   w->fgeo = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FGEO4));
   w->fdx = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FDX4));
+  w->fflux = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FLUX4));
   w->inv_vol = reinterpret_cast<double *>(take(sizeof(double) * (size_t)w->nc));
+  w->inv_vol32 = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
 }
 
 template <int D>
-static cudaError_t setup(const fvh_mesh_view &m, workspace *w) {
-  carve<D>(w);
+static cudaError_t setup_d(const fvh_mesh_view &m, workspace *w, cudaStream_t st) {
   const int t = 256;
-  setup_cells<D><<<(m.num_cells + t - 1) / t, t>>>(m, *w);
-  setup_vertices<D><<<(m.num_vertices + t - 1) / t, t>>>(m, *w);
-  setup_faces<D><<<(m.num_faces + t - 1) / t, t>>>(m, *w);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  return e;
+  setup_cells<D><<<(m.num_cells + t - 1) / t, t, 0, st>>>(m, *w);
+  setup_vertices<D><<<(m.num_vertices + t - 1) / t, t, 0, st>>>(m, *w);
+  setup_faces<D><<<(m.num_faces + t - 1) / t, t, 0, st>>>(m, *w);
+  return cudaGetLastError();
 }
 
-fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) {
+cudaError_t setup_geometry(workspace *w, const fvh_mesh_view &m, cudaStream_t st) {
+  if (m.num_cells > w->nc || m.num_faces > w->nf || m.num_vertices > w->nv)
+    return cudaErrorInvalidValue;
+  return m.dim == 2 ? setup_d<2>(m, w, st) : setup_d<3>(m, w, st);
+}
+
+fvh_status create_capacity(int dim, int64_t cells, int64_t faces, int64_t vertices,
+                           workspace **out) {
   *out = nullptr;
+  if ((dim != 2 && dim != 3) || cells <= 0 || faces <= 0 || vertices <= 0 ||
+      cells > INT32_MAX || faces > INT32_MAX || vertices > INT32_MAX)
+    return FVH_ERR_INVALID_ARGUMENT;
   workspace *w = new (std::nothrow) workspace();
   if (!w) return FVH_ERR_OUT_OF_MEMORY;
-  w->dim = m.dim;
-  w->nc = m.num_cells;
-  w->nf = m.num_faces;
-  w->nv = m.num_vertices;
-  const size_t bytes = m.dim == 2 ? bytes_for<2>(w->nc, w->nf, w->nv)
-                                  : bytes_for<3>(w->nc, w->nf, w->nv);
+  w->dim = dim;
+  w->nc = (int)cells;
+  w->nf = (int)faces;
+  w->nv = (int)vertices;
+  const size_t bytes = dim == 2 ? bytes_for<2>(w->nc, w->nf, w->nv) : bytes_for<3>(w->nc, w->nf, w->nv);
   cudaError_t e = cudaMalloc(&w->base, bytes);
   if (e == cudaSuccess) e = cudaMemset(w->base, 0, bytes);
-  if (e == cudaSuccess) e = m.dim == 2 ? setup<2>(m, w) : setup<3>(m, w);
   if (e != cudaSuccess) {
     destroy(w);
     return e == cudaErrorMemoryAllocation ? FVH_ERR_OUT_OF_MEMORY : FVH_ERR_CUDA;
   }
-  (void)p;
+  if (dim == 2)
+    carve<2>(w);
+  else
+    carve<3>(w);
   *out = w;
+  return FVH_OK;
+}
+
+fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) {
+  (void)p;
+  const fvh_status r = create_capacity(m.dim, m.num_cells, m.num_faces, m.num_vertices, out);
+  if (r != FVH_OK) return r;
+  cudaError_t e = setup_geometry(*out, m, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    destroy(*out);
+    *out = nullptr;
+    return FVH_ERR_CUDA;
+  }
   return FVH_OK;
 }
 
@@ -580,33 +817,71 @@ void destroy(workspace *w) {
   delete w;
 }
 
-template <int D, int KIND, bool SECOND>
-static void launch_stage(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
-                         const fvh_state_view &s, double *t, const double *dt, int stage,
-                         fvh_device_status *status, cudaStream_t st, const launch_mark &mark) {
-  const int nb = (m.num_cells + kCellThreads - 1) / kCellThreads;
+template <int D, int KIND, bool SECOND, int BS>
+static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                            const fvh_state_view &s, const problem_map &pm, int stage,
+                            int cpt, int schedule, cudaStream_t st, const launch_mark &mark) {
+  const long long per = (long long)BS * cpt;
+  const int nb = (int)((m.num_cells + per - 1) / per);
   const float4 *pk_in = stage == 0 ? w->pack : w->pack2;
   float4 *pk_out = stage == 0 ? w->pack2 : nullptr;
   if (SECOND) {
     if (p.limiter == FVH_LIMITER_NONE)
-      gradients_kernel<D, false><<<nb, kCellThreads, 0, st>>>(m, *w, pk_in);
+      gradients_kernel<D, false, BS><<<nb, BS, 0, st>>>(m, *w, pk_in);
     else
-      gradients_kernel<D, true><<<nb, kCellThreads, 0, st>>>(m, *w, pk_in);
+      gradients_kernel<D, true, BS><<<nb, BS, 0, st>>>(m, *w, pk_in);
     mark("gradients");
   }
-  flux_update_kernel<D, KIND, SECOND><<<nb, kCellThreads, 0, st>>>(
-      m, s, *w, pk_in, pk_out, dt, 0.5, p.gamma, p.cv, p.recon_swap_ep, p.boundary, t, status);
-  mark("flux_update");
+  const double gm1 = p.gamma - 1.0, inv_cv = 1.0 / p.cv;
+  const float ggm1 = (float)(p.gamma * (p.gamma - 1.0));
+  if (schedule == 1) {
+    const int nbf = (int)((m.num_faces + per - 1) / per);
+    face_flux_kernel<D, KIND, SECOND, BS><<<nbf, BS, 0, st>>>(m, *w, pk_in, p.recon_swap_ep,
+                                                               p.boundary);
+    mark("face_flux");
+    gather_update_kernel<D, BS><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, 0.5, gm1, ggm1, inv_cv);
+    mark("gather_update");
+  } else {
+    flux_update_kernel<D, KIND, SECOND, BS><<<nb, BS, 0, st>>>(
+        m, s, *w, pk_in, pk_out, pm, 0.5, gm1, ggm1, inv_cv, p.recon_swap_ep, p.boundary);
+    mark("flux_update");
+  }
+}
+
+template <int D, int KIND, bool SECOND>
+static void launch_stage(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                         const fvh_state_view &s, const problem_map &pm, int stage,
+                         const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
+  if (sh.block == 256)
+    launch_stage_bs<D, KIND, SECOND, 256>(w, m, p, s, pm, stage, sh.cells_per_thread,
+                                          sh.schedule, st, mark);
+  else
+    launch_stage_bs<D, KIND, SECOND, 128>(w, m, p, s, pm, stage, sh.cells_per_thread,
+                                          sh.schedule, st, mark);
 }
 
 template <int D, int KIND>
 static void launch_stage_k(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
-                           const fvh_state_view &s, double *t, const double *dt, int stage,
-                           fvh_device_status *status, cudaStream_t st, const launch_mark &mark) {
+                           const fvh_state_view &s, const problem_map &pm, int stage,
+                           const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
   if (p.order == 1)
-    launch_stage<D, KIND, false>(w, m, p, s, t, dt, stage, status, st, mark);
+    launch_stage<D, KIND, false>(w, m, p, s, pm, stage, sh, st, mark);
   else
-    launch_stage<D, KIND, true>(w, m, p, s, t, dt, stage, status, st, mark);
+    launch_stage<D, KIND, true>(w, m, p, s, pm, stage, sh, st, mark);
+}
+
+template <int D>
+static void launch_stages(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                          const fvh_state_view &s, const problem_map &pm,
+                          const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
+  for (int stage = 0; stage < 2; ++stage) {
+    if (p.flux_kind == FVH_FLUX_RUSANOV)
+      launch_stage_k<D, FVH_FLUX_RUSANOV>(w, m, p, s, pm, stage, sh, st, mark);
+    else if (p.flux_kind == FVH_FLUX_HLLC)
+      launch_stage_k<D, FVH_FLUX_HLLC>(w, m, p, s, pm, stage, sh, st, mark);
+    else
+      launch_stage_k<D, FVH_FLUX_HLLE>(w, m, p, s, pm, stage, sh, st, mark);
+  }
 }
 
 template <int D>
@@ -618,14 +893,11 @@ static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params
   mark("pack_dt");
   dt_final_kernel<<<1, kDtThreads, 0, st>>>(partial, dt_blocks, p, t, dt, status);
   mark("dt_final");
-  for (int stage = 0; stage < 2; ++stage) {
-    if (p.flux_kind == FVH_FLUX_RUSANOV)
-      launch_stage_k<D, FVH_FLUX_RUSANOV>(w, m, p, s, t, dt, stage, status, st, mark);
-    else if (p.flux_kind == FVH_FLUX_HLLC)
-      launch_stage_k<D, FVH_FLUX_HLLC>(w, m, p, s, t, dt, stage, status, st, mark);
-    else
-      launch_stage_k<D, FVH_FLUX_HLLE>(w, m, p, s, t, dt, stage, status, st, mark);
-  }
+  problem_map pm;
+  pm.dt = dt;
+  pm.t = t;
+  pm.status = status;
+  launch_stages<D>(w, m, p, s, pm, launch_shape(), st, mark);
   return cudaGetLastError();
 }
 
@@ -637,7 +909,33 @@ cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                     : step_d<3>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark);
 }
 
-int launches_per_step(const fvh_params &p) { return p.order == 1 ? 4 : 6; }
+template <int D>
+static cudaError_t step_batch_d(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                                const fvh_state_view &s, const problem_map &pm,
+                                const launch_shape &sh, cudaStream_t st,
+                                const launch_mark &mark) {
+  const int nb = (m.num_cells + kDtThreads - 1) / kDtThreads;
+  pack_dt_batch_kernel<D><<<nb, kDtThreads, 0, st>>>(m, s, *w, pm);
+  mark("pack_dt");
+  dt_final_batch_kernel<<<(pm.nproblems + 127) / 128, 128, 0, st>>>(pm, 0);
+  mark("dt_final");
+  launch_stages<D>(w, m, p, s, pm, sh, st, mark);
+  return cudaGetLastError();
+}
+
+cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                       const fvh_state_view &s, const problem_map &pm,
+                       const launch_shape &shape, cudaStream_t st, const launch_mark &mark) {
+  return m.dim == 2 ? step_batch_d<2>(w, m, p, s, pm, shape, st, mark)
+                    : step_batch_d<3>(w, m, p, s, pm, shape, st, mark);
+}
+
+int launches_per_step(const fvh_params &p, const launch_shape &sh) {
+  const int per_stage = (p.order == 1 ? 0 : 1) + (sh.schedule == 1 ? 2 : 1);
+  return 2 + 2 * per_stage;
+}
+
+int launches_per_step(const fvh_params &p) { return launches_per_step(p, launch_shape()); }
 
 }  // namespace mixed
 }  // namespace fvh

@@ -14,6 +14,12 @@ struct workspace;
 fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out);
 void destroy(workspace *w);
 
+// Workspace sized for up to (cells, faces, vertices); setup_geometry derives
+// its FP32 geometry from a mesh within those bounds (stream-ordered).
+fvh_status create_capacity(int dim, int64_t cells, int64_t faces, int64_t vertices,
+                           workspace **out);
+cudaError_t setup_geometry(workspace *w, const fvh_mesh_view &m, cudaStream_t st);
+
 // Called after each kernel launch of a step when profiling (name is static).
 struct launch_mark {
   void (*fn)(void *ctx, const char *name) = nullptr;
@@ -31,6 +37,35 @@ cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
 
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
+
+// Independent problems concatenated into one mesh: problem k owns the cells
+// [first_cell[k], first_cell[k+1]).  All arrays are device memory.
+struct problem_map {
+  const int *cell_problem = nullptr;   // [cells]; null: one problem
+  const int *first_cell = nullptr;     // [P+1]
+  int nproblems = 1;
+  const double *cfl = nullptr;         // [P]
+  const double *final_time = nullptr;  // [P]
+  double *t = nullptr;                 // [P] solution time
+  double *dt = nullptr;                // [P]
+  unsigned *dtinv_bits = nullptr;      // [P] max (a+|v.n|)A/V as FP32 bits; reset each step
+  fvh_device_status *status = nullptr; // [P]
+};
+
+// Launch shape of the cell kernels (picked by the autotuner).
+struct launch_shape {
+  int block = 128;          // threads per block: 128 or 256
+  int cells_per_thread = 1; // grid = ceil(cells / (block * cells_per_thread)), grid-stride
+  int schedule = 0;         // 0: cell-centric (each cell evaluates its faces' fluxes);
+                            // 1: one flux per face into an array, then a cell gather
+};
+int launches_per_step(const fvh_params &p, const launch_shape &sh);
+
+// One time step of every problem of the batch (per-problem dt and time).
+cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
+                       const fvh_state_view &s, const problem_map &pm,
+                       const launch_shape &shape, cudaStream_t st,
+                       const launch_mark &mark = launch_mark());
 
 }  // namespace mixed
 }  // namespace fvh

@@ -147,11 +147,30 @@ __device__ __forceinline__ void hllc(const prim<D> &l, const prim<D> &r,
 }
 
 // ---------------------------------------------------------------------------
-// dt: per-block maxima of (a + |v.n|) / (V/A), then one block finishes.
+// Order-preserving integer keys of doubles.  Comparisons, minima and maxima of
+// doubles run on the integer pipe through these keys (the FP64 pipe of this
+// chip is narrow).  key(a) < key(b) exactly when a < b for non-NaN values;
+// -0 and +0 share the key of +0, so a minimum or maximum can differ from the
+// floating-point one only in the sign of a zero.
 // ---------------------------------------------------------------------------
-template <int D>
+__device__ __forceinline__ long long okey(double x) {
+  long long b = __double_as_longlong(x);
+  b = (b == (long long)0x8000000000000000ull) ? 0ll : b;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double from_okey(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+
+// ---------------------------------------------------------------------------
+// dt: per-block maxima of (a + |v.n|) / (V/A), then one block finishes.
+// With PRE the V/A of each (cell, face) slot comes from a table built once per
+// mesh by the same division.
+// ---------------------------------------------------------------------------
+template <int D, bool PRE>
 __global__ void __launch_bounds__(kDtThreads)
-dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial) {
+dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial,
+                  const double *__restrict__ slot_dx) {
   double dt_inv = 0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.num_cells;
        c += gridDim.x * blockDim.x) {
@@ -159,7 +178,7 @@ dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial
 #pragma unroll
     for (int i = 0; i < D; ++i) v[i] = s.velocity[i][c];
     const double a = s.sound_speed[c];
-    const double vol = m.cell_volume[c];
+    const double vol = PRE ? 0.0 : m.cell_volume[c];
     const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
     for (int q = q0; q < q1; ++q) {
       int f = m.cell_faces[q];
@@ -167,7 +186,7 @@ dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial
       double n[D];
 #pragma unroll
       for (int i = 0; i < D; ++i) n[i] = m.face_normal[i][f];
-      const double delta_x = vol / m.face_area[f];
+      const double delta_x = PRE ? slot_dx[q] : vol / m.face_area[f];
       const double dti = (a + fabs(dot<D>(v, n))) / delta_x;
       dt_inv = smax(dti, dt_inv);
     }
@@ -196,19 +215,100 @@ dt_final_kernel(const double *partial, int nblocks, fvh_params p,
 }
 
 // ---------------------------------------------------------------------------
-// gradients + Barth-Jespersen vertex limiter (tasks.h:145-321)
+// Geometry-only tables built once per mesh for the solver (same operations in
+// the same order as the on-the-fly code, so the values are identical).
 // ---------------------------------------------------------------------------
-template <int D, bool LIMIT>
+template <int D>
+__global__ void slot_dx_kernel(const fvh_mesh_view m, double *slot_dx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.num_cells) return;
+  const double vol = m.cell_volume[c];
+  for (int q = m.cell_face_offsets[c]; q < m.cell_face_offsets[c + 1]; ++q) {
+    int f = m.cell_faces[q];
+    f = f < 0 ? ~f : f;
+    slot_dx[q] = vol / m.face_area[f];
+  }
+}
+
+// lsq record per cell: 2D (a00 a01 a11 denom); 3D (a00 a01 a02 a11 a12 a22
+// min1 min2 min3 denom), tasks.h:210-228 and :250-261
+template <int D>
+struct lsq_width {
+  static constexpr int value = D == 2 ? 4 : 10;
+};
+
+template <int D>
+__device__ __forceinline__ void lsq_matrix(const fvh_mesh_view &m, int c0, double *r) {
+  double x0[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
+  double dxdx[6] = {0, 0, 0, 0, 0, 0};
+  for (int q = m.cell_nbr_offsets[c0]; q < m.cell_nbr_offsets[c0 + 1]; ++q) {
+    const int c1 = m.cell_nbrs[q];
+    double dx[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dx[d] = m.cell_centroid[d][c1] - x0[d];
+    if (D == 2) {
+      dxdx[0] += dx[0] * dx[0];
+      dxdx[1] += dx[0] * dx[1];
+      dxdx[2] += dx[1] * dx[1];
+    } else {
+      dxdx[0] += dx[0] * dx[0];
+      dxdx[1] += dx[0] * dx[1];
+      dxdx[2] += dx[0] * dx[D - 1];
+      dxdx[3] += dx[1] * dx[1];
+      dxdx[4] += dx[1] * dx[D - 1];
+      dxdx[5] += dx[D - 1] * dx[D - 1];
+    }
+  }
+  if (D == 2) {
+    r[0] = dxdx[0];
+    r[1] = dxdx[1];
+    r[2] = dxdx[2];
+    r[3] = 1 / (dxdx[0] * dxdx[2] - dxdx[1] * dxdx[1]);
+  } else {
+    const double a00 = dxdx[0], a01 = dxdx[1], a02 = dxdx[2], a11 = dxdx[3],
+                 a12 = dxdx[4], a22 = dxdx[5];
+    const double min1 = a11 * a22 - a12 * a12;
+    const double min2 = a01 * a22 - a12 * a02;
+    const double min3 = a01 * a12 - a11 * a02;
+    for (int k = 0; k < 6; ++k) r[k] = dxdx[k];
+    r[6] = min1;
+    r[7] = min2;
+    r[8] = min3;
+    r[9] = 1 / (a00 * min1 - a01 * min2 + a02 * min3);
+  }
+}
+
+template <int D>
+__global__ void lsq_kernel(const fvh_mesh_view m, double *lsq) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.num_cells) return;
+  constexpr int W = lsq_width<D>::value;
+  double r[W];
+  lsq_matrix<D>(m, c, r);
+#pragma unroll
+  for (int k = 0; k < W; ++k) lsq[(size_t)k * m.num_cells + c] = r[k];
+}
+
+// ---------------------------------------------------------------------------
+// gradients + Barth-Jespersen vertex limiter (tasks.h:145-321)
+// With PRE the geometry-only matrix terms come from the lsq table.
+// ---------------------------------------------------------------------------
+template <int D, bool LIMIT, bool PRE>
 __global__ void __launch_bounds__(kCellThreads)
-gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g) {
+gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
+                 const double *__restrict__ lsq) {
   constexpr int NV = D + 4;
+  constexpr int W = lsq_width<D>::value;
   constexpr double tol = 1.e-9;
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (c0 >= m.num_cells) return;
   double x0[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
-  double u0[NV], umin[NV], umax[NV];
+  double u0[NV];
+  long long kmin[NV], kmax[NV];  // umin / umax as order keys
   {
     int i = 0;
     u0[i++] = s.density[c0];
@@ -219,8 +319,7 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
     u0[i++] = s.sound_speed[c0];
   }
 #pragma unroll
-  for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
-  double dxdx[6] = {0, 0, 0, 0, 0, 0};  // 00 01 11 (2D) / 00 01 02 11 12 22 (3D)
+  for (int k = 0; k < NV; ++k) kmin[k] = kmax[k] = okey(u0[k]);
   double dudx[NV][D];
 #pragma unroll
   for (int k = 0; k < NV; ++k)
@@ -239,49 +338,37 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
       u1[i++] = s.pressure[c1];
       u1[i++] = s.sound_speed[c1];
     }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      umin[k] = smin(u1[k], umin[k]);
-      umax[k] = smax(u1[k], umax[k]);
-    }
     double dx[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) dx[d] = m.cell_centroid[d][c1] - x0[d];
-    if (D == 2) {
-      dxdx[0] += dx[0] * dx[0];
-      dxdx[1] += dx[0] * dx[1];
-      dxdx[2] += dx[1] * dx[1];
-    } else {
-      dxdx[0] += dx[0] * dx[0];
-      dxdx[1] += dx[0] * dx[1];
-      dxdx[2] += dx[0] * dx[D - 1];
-      dxdx[3] += dx[1] * dx[1];
-      dxdx[4] += dx[1] * dx[D - 1];
-      dxdx[5] += dx[D - 1] * dx[D - 1];
-    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
+      const long long k1 = okey(u1[k]);
+      kmin[k] = (k1 < kmin[k]) ? k1 : kmin[k];  // std::min(u1, umin)
+      kmax[k] = (kmax[k] < k1) ? k1 : kmax[k];  // std::max(u1, umax)
       const double du = u1[k] - u0[k];
 #pragma unroll
       for (int j = 0; j < D; ++j) dudx[k][j] += du * dx[j];
     }
   }
+  double r[W];
+  if (PRE) {
+#pragma unroll
+    for (int k = 0; k < W; ++k) r[k] = lsq[(size_t)k * m.num_cells + c0];
+  } else {
+    lsq_matrix<D>(m, c0, r);
+  }
   double gu[NV][D];
   if (D == 2) {
-    const double a00 = dxdx[0], a01 = dxdx[1], a11 = dxdx[2];
-    const double denom = 1 / (a00 * a11 - a01 * a01);
+    const double a00 = r[0], a01 = r[1], a11 = r[2], denom = r[3];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       gu[k][0] = (dudx[k][0] * a11 - dudx[k][1] * a01) * denom;
       gu[k][1] = (dudx[k][1] * a00 - dudx[k][0] * a01) * denom;
     }
   } else {
-    const double a00 = dxdx[0], a01 = dxdx[1], a02 = dxdx[2], a11 = dxdx[3],
-                 a12 = dxdx[4], a22 = dxdx[5];
-    const double min1 = a11 * a22 - a12 * a12;
-    const double min2 = a01 * a22 - a12 * a02;
-    const double min3 = a01 * a12 - a11 * a02;
-    const double denom = 1 / (a00 * min1 - a01 * min2 + a02 * min3);
+    const double a00 = r[0], a01 = r[1], a02 = r[2], a11 = r[3], a12 = r[4], a22 = r[5];
+    const double min1 = r[6], min2 = r[7], min3 = r[W - 2], denom = r[W - 1];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       const double b0 = dudx[k][0], b1 = dudx[k][1], b2 = dudx[k][D - 1];
@@ -294,16 +381,14 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
     // phi_k = min over vertices of (umax-u0)/du or (umin-u0)/du.  Correctly
     // rounded division is monotone in the divisor, so for each variable only
     // the largest du > tol and the smallest du < -tol can set the minimum; the
-    // result equals the reference's per-vertex minimum bit for bit.
-    double dpos[NV], dneg[NV];
+    // result equals the reference's per-vertex minimum.
+    const long long ktol = okey(tol), kntol = okey(-tol);
+    long long kpos[NV], kneg[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      dpos[k] = 0;
-      dneg[k] = 0;
-    }
+    for (int k = 0; k < NV; ++k) kpos[k] = kneg[k] = 0;
     const int r0 = m.cell_vertex_offsets[c0], r1 = m.cell_vertex_offsets[c0 + 1];
-    for (int r = r0; r < r1; ++r) {
-      const int vtx = m.cell_vertices[r];
+    for (int rr = r0; rr < r1; ++rr) {
+      const int vtx = m.cell_vertices[rr];
       double dxv[D];
 #pragma unroll
       for (int i = 0; i < D; ++i) dxv[i] = m.vertex_coord[i][vtx] - x0[i];
@@ -312,19 +397,28 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
         double u1 = u0[k];
 #pragma unroll
         for (int i = 0; i < D; ++i) u1 += dxv[i] * gu[k][i];
-        const double du = u1 - u0[k];
-        if (du > tol) dpos[k] = smax(du, dpos[k]);
-        else if (du < -tol) dneg[k] = smin(du, dneg[k]);
+        const long long kd = okey(u1 - u0[k]);
+        if (kd > ktol) kpos[k] = (kpos[k] < kd) ? kd : kpos[k];
+        else if (kd < kntol) kneg[k] = (kd < kneg[k]) ? kd : kneg[k];
       }
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double phi = 1;
-      if (dpos[k] > tol) phi = smin(phi, (umax[k] - u0[k]) / dpos[k]);
-      if (dneg[k] < -tol) phi = smin(phi, (umin[k] - u0[k]) / dneg[k]);
-      phi = smax(phi, 0.0);
+      long long kphi = okey(1.0);
+      if (kpos[k] > ktol) {
+        const long long kq = okey((from_okey(kmax[k]) - u0[k]) / from_okey(kpos[k]));
+        kphi = (kq < kphi) ? kq : kphi;
+      }
+      if (kneg[k] < kntol) {
+        const long long kq = okey((from_okey(kmin[k]) - u0[k]) / from_okey(kneg[k]));
+        kphi = (kq < kphi) ? kq : kphi;
+      }
+      kphi = (kphi < 0) ? 0 : kphi;  // std::max(phi, 0)
+      if (kphi != okey(1.0)) {
+        const double phi = from_okey(kphi);
 #pragma unroll
-      for (int i = 0; i < D; ++i) gu[k][i] *= phi;
+        for (int i = 0; i < D; ++i) gu[k][i] *= phi;
+      }
     }
   }
 #pragma unroll
@@ -462,7 +556,7 @@ update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_vie
   for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
   s.internal_energy[c] = e;
   s.pressure[c] = (gamma - 1.0) * mass * e;
-  s.temperature[c] = e / cv;
+  s.temperature[c] = cv == 1.0 ? e : e / cv;  // x / 1 == x exactly
   s.sound_speed[c] = sqrt(gamma * (gamma - 1.0) * e);
   if (e < 0 || mass < 0) atomicMin(status, status_key(c, FVH_ERR_NEGATIVE_STATE));
 }
@@ -474,8 +568,11 @@ template <int D>
 cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
                       const fvh_params &p, const double *soln_time, double *dt,
                       double *partial, int nblocks, fvh_device_status *status,
-                      cudaStream_t st) {
-  dt_partial_kernel<D><<<nblocks, kDtThreads, 0, st>>>(m, s, partial);
+                      cudaStream_t st, const double *slot_dx) {
+  if (slot_dx)
+    dt_partial_kernel<D, true><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, slot_dx);
+  else
+    dt_partial_kernel<D, false><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, nullptr);
   dt_final_kernel<<<1, kDtThreads, 0, st>>>(partial, nblocks, p, soln_time, dt, status);
   return cudaGetLastError();
 }
@@ -483,14 +580,32 @@ cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
 template <int D>
 cudaError_t launch_gradients(const fvh_mesh_view &m, const fvh_state_view &s,
                              const fvh_gradient_view &g, const fvh_params &p,
-                             cudaStream_t st) {
+                             cudaStream_t st, const double *lsq) {
   const int nb = (m.num_cells + kCellThreads - 1) / kCellThreads;
-  if (p.limiter == FVH_LIMITER_NONE)
-    gradients_kernel<D, false><<<nb, kCellThreads, 0, st>>>(m, s, g);
-  else
-    gradients_kernel<D, true><<<nb, kCellThreads, 0, st>>>(m, s, g);
+  const bool lim = p.limiter != FVH_LIMITER_NONE;
+  if (lsq) {
+    if (lim)
+      gradients_kernel<D, true, true><<<nb, kCellThreads, 0, st>>>(m, s, g, lsq);
+    else
+      gradients_kernel<D, false, true><<<nb, kCellThreads, 0, st>>>(m, s, g, lsq);
+  } else {
+    if (lim)
+      gradients_kernel<D, true, false><<<nb, kCellThreads, 0, st>>>(m, s, g, nullptr);
+    else
+      gradients_kernel<D, false, false><<<nb, kCellThreads, 0, st>>>(m, s, g, nullptr);
+  }
   return cudaGetLastError();
 }
+
+template <int D>
+cudaError_t build_tables(const fvh_mesh_view &m, double *lsq, double *slot_dx) {
+  const int t = 128, nb = (m.num_cells + t - 1) / t;
+  lsq_kernel<D><<<nb, t>>>(m, lsq);
+  slot_dx_kernel<D><<<nb, t>>>(m, slot_dx);
+  return cudaGetLastError();
+}
+
+int lsq_doubles_per_cell(int dim) { return dim == 2 ? lsq_width<2>::value : lsq_width<3>::value; }
 
 template <int D, bool SECOND>
 static void launch_fluxes_kind(const fvh_mesh_view &m, const fvh_state_view &s,
@@ -530,10 +645,12 @@ cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const dou
 #define FVH_INSTANTIATE(D)                                                              \
   template cudaError_t launch_dt<D>(const fvh_mesh_view &, const fvh_state_view &,     \
                                     const fvh_params &, const double *, double *,      \
-                                    double *, int, fvh_device_status *, cudaStream_t); \
+                                    double *, int, fvh_device_status *, cudaStream_t,  \
+                                    const double *);                                   \
   template cudaError_t launch_gradients<D>(const fvh_mesh_view &, const fvh_state_view &, \
                                            const fvh_gradient_view &, const fvh_params &, \
-                                           cudaStream_t);                              \
+                                           cudaStream_t, const double *);              \
+  template cudaError_t build_tables<D>(const fvh_mesh_view &, double *, double *);     \
   template cudaError_t launch_fluxes<D>(const fvh_mesh_view &, const fvh_state_view &, \
                                         const fvh_gradient_view &, const fvh_flux_view &, \
                                         const fvh_params &, cudaStream_t);             \

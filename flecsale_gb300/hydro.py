@@ -138,6 +138,23 @@ def _declare(L: C.CDLL) -> None:
         "fvh_evaluate_time_step_noalloc": (C.c_int, [C.POINTER(MeshView), C.POINTER(StateView),
                                                      C.POINTER(Params), vp, vp, vp, vp]),
         "fvh_time_step_noalloc_max_cells": (C.c_int32, []),
+        "fvh_host_mesh_concat": (C.c_int, [C.c_int32, C.POINTER(vp), C.POINTER(vp)]),
+        "fvh_batch_create": (C.c_int, [C.POINTER(Params), C.c_int64, C.c_int64, C.c_int64,
+                                       C.c_int32, C.POINTER(vp)]),
+        "fvh_batch_destroy": (None, [vp]),
+        "fvh_batch_assign": (C.c_int, [vp, C.c_int32, C.POINTER(vp), _dp, _dp,
+                                       C.POINTER(C.c_int32), vp]),
+        "fvh_batch_set_state": (C.c_int, [vp, C.c_int32, _dp, C.c_double, vp]),
+        "fvh_batch_get_state": (C.c_int, [vp, C.c_int32, _dp, vp]),
+        "fvh_batch_step": (C.c_int, [vp, C.c_int32, vp]),
+        "fvh_batch_query": (C.c_int, [vp, _dp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), vp]),
+        "fvh_batch_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
+        "fvh_batch_num_problems": (C.c_int32, [vp]),
+        "fvh_batch_autotune": (C.c_int, [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_double), vp]),
+        "fvh_batch_num_cells": (C.c_int64, [vp]),
+        "fvh_batch_launches_per_step": (C.c_int32, [vp]),
         "fvh_solver_profile": (C.c_int, [vp, C.POINTER(StateView), C.c_int32, C.c_int32,
                                          C.POINTER(C.c_char_p), _dp, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), vp]),
@@ -448,6 +465,85 @@ class Solver:
     def close(self):
         if self._h and _LIB is not None:
             _LIB.fvh_solver_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+
+class Batch:
+    """fvh_batch: independent meshes advanced together (mixed precision)."""
+
+    def __init__(self, params: Params, max_cells: int, max_faces: int, max_vertices: int,
+                 max_problems: int):
+        self.params = params
+        self.dim = params.dim
+        self._h = C.c_void_p()
+        check(lib().fvh_batch_create(C.byref(params), max_cells, max_faces, max_vertices,
+                                     max_problems, C.byref(self._h)), "fvh_batch_create")
+        self.meshes: list = []
+
+    @classmethod
+    def for_meshes(cls, params: Params, meshes, slack: float = 1.0, max_problems=None):
+        nc = sum(m.num_cells for m in meshes)
+        nf = sum(m.num_faces for m in meshes)
+        nv = sum(m.num_vertices for m in meshes)
+        return cls(params, int(nc * slack) + 1, int(nf * slack) + 1, int(nv * slack) + 1,
+                   max_problems or len(meshes))
+
+    def assign(self, meshes, cfl, final_time, keep=None, stream=None) -> None:
+        n = len(meshes)
+        arr = (C.c_void_p * n)(*[m._h for m in meshes])
+        cf = np.ascontiguousarray(np.broadcast_to(np.asarray(cfl, np.float64), (n,)))
+        tf = np.ascontiguousarray(np.broadcast_to(np.asarray(final_time, np.float64), (n,)))
+        kp = None if keep is None else (C.c_int32 * n)(*keep)
+        check(lib().fvh_batch_assign(self._h, n, arr, _dptr(cf), _dptr(tf), kp,
+                                     stream_handle(stream)), "fvh_batch_assign")
+        self.meshes = list(meshes)
+
+    def set_state(self, k: int, planes: np.ndarray, t: float = 0.0, stream=None) -> None:
+        planes = np.ascontiguousarray(planes[:5 + self.dim], np.float64)
+        check(lib().fvh_batch_set_state(self._h, k, _dptr(planes), t, stream_handle(stream)),
+              "fvh_batch_set_state")
+
+    def get_state(self, k: int, stream=None) -> np.ndarray:
+        out = np.empty((5 + self.dim, self.meshes[k].num_cells), np.float64)
+        check(lib().fvh_batch_get_state(self._h, k, _dptr(out), stream_handle(stream)),
+              "fvh_batch_get_state")
+        return out
+
+    def step(self, nsteps: int = 1, stream=None) -> None:
+        check(lib().fvh_batch_step(self._h, nsteps, stream_handle(stream)), "fvh_batch_step")
+
+    def query(self, stream=None):
+        n = lib().fvh_batch_num_problems(self._h)
+        t = np.zeros(n)
+        codes = (C.c_int32 * n)()
+        bad = (C.c_int64 * n)()
+        lib().fvh_batch_query(self._h, _dptr(t), codes, bad, stream_handle(stream))
+        return t, np.array(codes[:], np.int32), np.array(bad[:], np.int64)
+
+    def set_shape(self, block: int, cells_per_thread: int, schedule: int = 0) -> None:
+        check(lib().fvh_batch_set_shape(self._h, block, cells_per_thread, schedule),
+              "fvh_batch_set_shape")
+
+    def autotune(self, trial_steps: int = 3, use_cache: bool = True, stream=None) -> dict:
+        blk, cpt, sch, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        check(lib().fvh_batch_autotune(self._h, trial_steps, 1 if use_cache else 0, C.byref(blk),
+                                       C.byref(cpt), C.byref(sch), C.byref(ms),
+                                       stream_handle(stream)), "fvh_batch_autotune")
+        return {"block": blk.value, "cells_per_thread": cpt.value, "schedule": sch.value,
+                "ms_per_step": ms.value}
+
+    @property
+    def num_cells(self) -> int:
+        return lib().fvh_batch_num_cells(self._h)
+
+    def launches_per_step(self) -> int:
+        return lib().fvh_batch_launches_per_step(self._h)
+
+    def close(self):
+        if self._h and _LIB is not None:
+            _LIB.fvh_batch_destroy(self._h)
             self._h = None
 
     __del__ = close

@@ -320,6 +320,12 @@ fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
 
 void fvh_host_mesh_destroy(fvh_host_mesh *m);
 
+/* Concatenate meshes of one dimension into one block-diagonal mesh: cells,
+ * faces and vertices of mesh k follow those of meshes 0..k-1, with all indices
+ * shifted; no connectivity is added between meshes. */
+fvh_status fvh_host_mesh_concat(int32_t n, const fvh_host_mesh *const *meshes,
+                                fvh_host_mesh **out);
+
 /* Host-memory view of the mesh arrays (valid while m lives). */
 fvh_status fvh_host_mesh_view(const fvh_host_mesh *m, fvh_mesh_view *out);
 
@@ -382,6 +388,73 @@ fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim,
 fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_state,
                                    double *host_planes, int64_t nsteps,
                                    double *soln_time, fvh_stream_t stream);
+
+/* ------------------------------------------------------------------------- */
+/* Batched form: independent meshes advanced together (mixed precision)      */
+/* ------------------------------------------------------------------------- */
+/* No counterpart in the reference, whose driver advances one mesh per colour.
+ * A batch holds up to max_problems meshes with at most the given total cells,
+ * faces and vertices, concatenated block-diagonally in device memory; each
+ * problem has its own CFL number, final time, solution time, dt and status.
+ * One fvh_batch_step advances every problem by nsteps steps in one CUDA-graph
+ * launch; a problem at its final time gets dt = 0.  Results of a problem do not
+ * depend on the other problems in the batch. */
+typedef struct fvh_batch fvh_batch;
+
+/* params: shared scheme (precision must be FVH_PRECISION_MIXED; dim, flux,
+ * limiter, order, swap, boundary, gamma, cv). */
+fvh_status fvh_batch_create(const fvh_params *params, int64_t max_cells,
+                            int64_t max_faces, int64_t max_vertices,
+                            int32_t max_problems, fvh_batch **out);
+void fvh_batch_destroy(fvh_batch *b);
+
+/* Replace the batch's problems by n meshes.  keep[k] >= 0 carries the device
+ * state and solution time of problem keep[k] of the previous assignment (same
+ * cell count) into new problem k; keep == NULL or keep[k] < 0 leaves problem k
+ * to be set with fvh_batch_set_state.  Synchronises the stream. */
+fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const *meshes,
+                            const double *cfl, const double *final_time,
+                            const int32_t *keep, fvh_stream_t stream);
+
+/* Host planes (d, v[0..dim), e, p, T, a; one plane per field, problem cells)
+ * in and out of problem k; set_state also sets its solution time.  Both
+ * synchronise the stream. */
+fvh_status fvh_batch_set_state(fvh_batch *b, int32_t k, const double *host_planes,
+                               double t, fvh_stream_t stream);
+fvh_status fvh_batch_get_state(fvh_batch *b, int32_t k, double *host_planes,
+                               fvh_stream_t stream);
+
+/* Advance every problem nsteps steps (one CUDA graph per step count). */
+fvh_status fvh_batch_step(fvh_batch *b, int32_t nsteps, fvh_stream_t stream);
+
+/* Synchronise; per problem: solution time, status code and first bad cell
+ * (problem-local id).  Returns the first non-OK code, if any. */
+fvh_status fvh_batch_query(fvh_batch *b, double *times, int32_t *codes,
+                           int64_t *bad_cells, fvh_stream_t stream);
+
+/* Launch shape of the cell kernels: threads per block (128 or 256), cells per
+ * thread (1..8) and flux schedule (0: each cell evaluates the fluxes of its
+ * faces; 1: one flux per face into an array, then a cell-centric gather).  All
+ * shapes give the same results bit for bit. */
+fvh_status fvh_batch_set_shape(fvh_batch *b, int32_t block, int32_t cells_per_thread,
+                               int32_t schedule);
+
+/* Autotuner: times each launch shape (threads per block x cells per thread x
+ * schedule) for trial_steps steps on the current problems, keeps the fastest
+ * and restores the state, times and status words, so tuning does not change
+ * the results.  The winner is appended to a cache file (FVH_AUTOTUNE_CACHE,
+ * default $HOME/.cache/flecsale_gb300_autotune.txt) keyed by device, scheme
+ * and size class; with use_cache != 0 a cached entry is applied without
+ * measuring (best_ms_per_step is then -1).  Allocates a temporary copy of the
+ * state. */
+fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cache,
+                              int32_t *block, int32_t *cells_per_thread,
+                              int32_t *schedule, double *best_ms_per_step,
+                              fvh_stream_t stream);
+
+int32_t fvh_batch_num_problems(const fvh_batch *b);
+int64_t fvh_batch_num_cells(const fvh_batch *b);
+int32_t fvh_batch_launches_per_step(const fvh_batch *b);
 
 #ifdef __cplusplus
 }
