@@ -286,6 +286,81 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
                       "KH shear layer / four-quadrant / Sod, HLLC, outflow, CFL 0.4, mixed precision"}
 
 
+def run_serving(torch, stream, batched_rate: float, seconds: float, seed: int = 4) -> dict:
+    """Poisson arrivals of 2D KH / four-quadrant / Sod requests (sides
+    log-uniform 64..2048, end times uniform 0.05..0.3) at a rate that loads the
+    device to ~80% of its measured batched throughput; continuous batching."""
+    import flecsale_gb300.hydro as H
+    from flecsale_gb300 import serve
+    # mean work per request ~ 6 * E[side^3] * E[t_end] zone-updates (dt ~ 0.4 h / 2.4)
+    lo, hi = 64.0, 2048.0
+    e_side3 = (hi ** 3 - lo ** 3) / (3.0 * np.log(hi / lo))
+    work = 6.0 * e_side3 * 0.175
+    rate = 0.8 * batched_rate / work
+    reqs = serve.poisson_requests(rate, seconds, seed)
+    p = H.make_params(2, flux="hllc", precision="mixed", boundary="outflow", cfl=0.4,
+                      final_time=1.0e9)
+    srv = serve.Server(p, max_cells=48_000_000, max_faces=97_000_000, max_vertices=49_000_000,
+                       max_problems=512, steps_per_launch=8, stream=stream)
+    rep = srv.run(reqs, time_limit=seconds + 120.0)
+    srv.close()
+    done = rep.pop("done")
+    small = sorted(done, key=lambda r: r.side)[:3]
+    l1 = [serve.fp64_rerun_l1(r, p) for r in small]
+    rep.update({"arrival_rate_per_s": rate, "arrival_window_s": seconds,
+                "l1_density_vs_fp64_rerun": {"requests": [r.side for r in small],
+                                             "max": max(l1) if l1 else None},
+                "config": "Poisson arrivals at ~80% of the measured batched throughput; sides "
+                          "log-uniform 64..2048 (cells 64^2..2048^2), t_end uniform [0.05, 0.3]; "
+                          "admission by device capacity (48M cells); 8 steps per graph launch"})
+    return rep
+
+
+def run_3d(torch, stream, n: int = 192, steps: int = 100) -> dict:
+    """192^3 hex shock box (inner cube [0,0.5]^3 at rho=1,p=1, rest 0.125/0.1),
+    jitter +-0.15h (seed 2), Rusanov, CFL 0.3, 100 steps: FP64 vs mixed."""
+    import flecsale_gb300.hydro as H
+    t0 = time.perf_counter()
+    mesh = H.HostMesh.box(3, (n, n, n), [0, 0, 0], [1, 1, 1], 0.15, 2)
+    build_s = time.perf_counter() - t0
+    kw = dict(flux="rusanov", cfl=0.3, final_time=1e9)
+    s0 = H.initial_state("inner_cube", mesh, H.make_params(3, **kw))
+    dm = H.DeviceMesh(mesh)
+    out = {}
+    res = {}
+    for form in ("fp64", "mixed"):
+        p = H.make_params(3, precision=form, **kw)
+        ds, sv = H.DeviceState(3, mesh.num_cells), None
+        sv = H.Solver(dm, p)
+        ds.upload(s0, stream)
+        sv.reset(0.0, stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            sv.step(ds, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        code, t, _ = sv.status(stream)
+        if code != 0:
+            raise RuntimeError(f"3d {form}: status {code}")
+        res[form] = ds.download(stream)
+        out[form] = {"value": mesh.num_cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                     "t_final": t}
+        del sv, ds
+    f, m = res["fp64"], res["mixed"]
+    E = lambda s: s[0] * (s[4] + 0.5 * (s[1] ** 2 + s[2] ** 2 + s[3] ** 2))
+    rel = lambda a, b: float(np.abs(a - b).sum() / np.abs(b).sum())
+    out.update({"cells": mesh.num_cells, "faces": mesh.num_faces, "steps": steps,
+                "host_mesh_build_s": build_s,
+                "l1_density": rel(m[0], f[0]), "linf_density": float(np.abs(m[0] - f[0]).max()),
+                "l1_total_energy": rel(E(m), E(f)), "linf_total_energy": float(np.abs(E(m) - E(f)).max()),
+                "config": f"{n}^3 hex on [0,1]^3 jittered +-0.15h (seed 2), inner cube, Rusanov, "
+                          f"CFL 0.3, walls, {steps} steps"})
+    return out
+
+
 def timed_steps(torch, solver, dstate, stream, K, dist):
     if dist:
         dist.barrier()
@@ -420,6 +495,11 @@ def run_ours(args):
     if not args.no_batch:
         line["batched"] = run_batched(torch, stream, min(args.steps, 50), args.warmup)
         line["batched_over_fp64"] = line["batched"]["value"] / line["plain_fp64"]["value"]
+        if args.serve_seconds > 0:
+            line["serving"] = run_serving(torch, stream, line["batched"]["value"],
+                                          args.serve_seconds)
+    if args.with_3d:
+        line["shock_box_3d"] = run_3d(torch, stream)
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mesh, p64, state0)
     print(json.dumps(line), flush=True)
@@ -436,6 +516,10 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-problem batched form")
+    ap.add_argument("--with-3d", action="store_true",
+                    help="also run the 192^3 3D shock box, FP64 vs mixed (100 steps)")
+    ap.add_argument("--serve-seconds", type=float, default=12.0,
+                    help="arrival window of the serving run (0 skips it)")
     ap.add_argument("--n", type=int, default=N_SIDE, help="mesh side (default 1024)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -654,6 +654,7 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
     const double delta_t = pm.dt[pr] * factor;
     if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
+    if (delta_t == 0.0) continue;  // finished problem: leave its state untouched
     // face sums in FP32 with error-free two-sum compensation (hi + lo carries
     // about 48 bits), one FP64 add per component afterwards
     float shi[D + 2], slo[D + 2];
@@ -700,6 +701,7 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
     const double delta_t = pm.dt[pr] * factor;
     if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
+    if (delta_t == 0.0) continue;  // finished problem: leave its state untouched
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
