@@ -204,6 +204,17 @@ def dist_setup(backend: str):
     return None, 1, 0, local
 
 
+def max_over_ranks(dist, value: float, device: str = "cuda") -> float:
+    """Maximum of a per-rank time over all ranks (all-reduce MAX); identity
+    without a process group."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -254,9 +265,9 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
     step, per-problem dt, launch shape picked by the autotuner."""
     import flecsale_gb300.hydro as H
     t0 = time.perf_counter()
+    from flecsale_gb300 import serve
     probs = batch_problems()
-    p = H.make_params(2, flux="hllc", precision="mixed", boundary="outflow", cfl=0.4,
-                      final_time=1.0e9)
+    p = serve.server_params()
     meshes = [m for m, _ in probs]
     b = H.Batch.for_meshes(p, meshes)
     b.assign(meshes, 0.4, 1.0e9, stream=stream)
@@ -283,7 +294,8 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
             "gpu_launches": b.launches_per_step() * steps,
             "autotuned_shape": tune, "host_setup_s": setup_s,
             "config": "512 independent 2D problems, cells log-uniform in [32^2, 512^2] (seed 3), "
-                      "KH shear layer / four-quadrant / Sod, HLLC, outflow, CFL 0.4, mixed precision"}
+                      "KH shear layer / four-quadrant / Sod, HLLC, outflow, textbook reconstruction, CFL 0.4, "
+                      "mixed precision"}
 
 
 def run_serving(torch, stream, batched_rate: float, seconds: float, seed: int = 4) -> dict:
@@ -298,8 +310,7 @@ def run_serving(torch, stream, batched_rate: float, seconds: float, seed: int = 
     work = 6.0 * e_side3 * 0.175
     rate = 0.8 * batched_rate / work
     reqs = serve.poisson_requests(rate, seconds, seed)
-    p = H.make_params(2, flux="hllc", precision="mixed", boundary="outflow", cfl=0.4,
-                      final_time=1.0e9)
+    p = serve.server_params()
     srv = serve.Server(p, max_cells=48_000_000, max_faces=97_000_000, max_vertices=49_000_000,
                        max_problems=512, steps_per_launch=8, stream=stream)
     rep = srv.run(reqs, time_limit=seconds + 120.0)
@@ -373,9 +384,7 @@ def timed_steps(torch, solver, dstate, stream, K, dist):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(dist, ms)
         dist.barrier()
     return ms
 
@@ -420,10 +429,7 @@ def run_ours(args):
     for _ in range(args.steps):
         t_sim = r["solver"].advance_host(r["state"], host, 1, t_sim, stream)
     e2e_s = time.perf_counter() - w0
-    if dist:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(dist, e2e_s)
 
     # per-kernel timings (CUDA events between launches on the stream)
     prof = {f: results[f]["solver"].profile(results[f]["state"], 10, stream) for f in results}

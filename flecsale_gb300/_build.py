@@ -30,6 +30,7 @@ CXX_COMMON = ["-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17",
 UNITS = [
     ("fvh_mesh.cpp", []),
     ("fvh_problems.cpp", []),
+    ("fvh_io.cpp", []),
     ("fvh_plain.cu", ["--fmad=false"]),
     ("fvh_mixed.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("fvh_capi.cu", []),

@@ -12,6 +12,7 @@
 // else is in the batch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -289,6 +290,207 @@ fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const 
   if (e == cudaSuccess) e = fvh::mixed::setup_geometry(b->ws, v, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors die below
   fvh_host_mesh_destroy(cat);
+  if (e != cudaSuccess) return from_cuda(e);
+  b->cur = nxt;
+  set_state_view(b);
+  b->first_cell = first;
+  b->nproblems = n;
+  drop_graphs(b);
+  return FVH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device-side assignment: problems already in device memory are concatenated
+// by gather kernels (indices shifted on the fly), so admitting or evicting a
+// request costs no host work proportional to the other requests' sizes.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct src_mesh {
+  fvh_mesh_view v;
+  int32_t c0, f0, v0, cf0, nb0, cv0;   // destination offsets
+  int32_t ncf, nnb, ncv;               // storage lengths
+  int32_t keep_from;                   // old first cell of a carried state, or -1
+};
+
+constexpr int kGatherThreads = 256, kGatherPerBlock = 256 * 16;
+
+// grid: x = problem, y = chunk of kGatherPerBlock elements
+__global__ void gather_cells(const src_mesh *src, fvh_mesh_view dst, int32_t *cell_problem,
+                             int dim) {
+  const src_mesh &s = src[blockIdx.x];
+  const int n = s.v.num_cells;
+  for (int i = blockIdx.y * kGatherPerBlock + threadIdx.x;
+       i < n && i < (int)(blockIdx.y + 1) * kGatherPerBlock; i += kGatherThreads) {
+    const int g = s.c0 + i;
+    cell_problem[g] = blockIdx.x;
+    const_cast<int32_t *>(dst.cell_face_offsets)[g] = s.v.cell_face_offsets[i] + s.cf0;
+    const_cast<int32_t *>(dst.cell_nbr_offsets)[g] = s.v.cell_nbr_offsets[i] + s.nb0;
+    const_cast<int32_t *>(dst.cell_vertex_offsets)[g] = s.v.cell_vertex_offsets[i] + s.cv0;
+    for (int d = 0; d < dim; ++d) const_cast<double *>(dst.cell_centroid[d])[g] = s.v.cell_centroid[d][i];
+    const_cast<double *>(dst.cell_volume)[g] = s.v.cell_volume[i];
+  }
+}
+
+__global__ void gather_faces(const src_mesh *src, fvh_mesh_view dst, int dim) {
+  const src_mesh &s = src[blockIdx.x];
+  const int n = s.v.num_faces;
+  for (int i = blockIdx.y * kGatherPerBlock + threadIdx.x;
+       i < n && i < (int)(blockIdx.y + 1) * kGatherPerBlock; i += kGatherThreads) {
+    const int g = s.f0 + i;
+    const int a = s.v.face_cells[2 * (size_t)i], b = s.v.face_cells[2 * (size_t)i + 1];
+    int32_t *fc = const_cast<int32_t *>(dst.face_cells);
+    fc[2 * (size_t)g] = a + s.c0;
+    fc[2 * (size_t)g + 1] = b < 0 ? -1 : b + s.c0;
+    for (int d = 0; d < dim; ++d) {
+      const_cast<double *>(dst.face_centroid[d])[g] = s.v.face_centroid[d][i];
+      const_cast<double *>(dst.face_normal[d])[g] = s.v.face_normal[d][i];
+    }
+    const_cast<double *>(dst.face_area)[g] = s.v.face_area[i];
+  }
+}
+
+__global__ void gather_vertices(const src_mesh *src, fvh_mesh_view dst, int dim) {
+  const src_mesh &s = src[blockIdx.x];
+  const int n = s.v.num_vertices;
+  for (int i = blockIdx.y * kGatherPerBlock + threadIdx.x;
+       i < n && i < (int)(blockIdx.y + 1) * kGatherPerBlock; i += kGatherThreads)
+    for (int d = 0; d < dim; ++d)
+      const_cast<double *>(dst.vertex_coord[d])[s.v0 + i] = s.v.vertex_coord[d][i];
+}
+
+// which = 0: cell_faces (signed face ids), 1: cell_nbrs, 2: cell_vertices
+__global__ void gather_csr(const src_mesh *src, fvh_mesh_view dst, int which) {
+  const src_mesh &s = src[blockIdx.x];
+  const int n = which == 0 ? s.ncf : which == 1 ? s.nnb : s.ncv;
+  const int32_t *in = which == 0 ? s.v.cell_faces : which == 1 ? s.v.cell_nbrs : s.v.cell_vertices;
+  int32_t *out = const_cast<int32_t *>(which == 0 ? dst.cell_faces
+                                       : which == 1 ? dst.cell_nbrs : dst.cell_vertices);
+  const int o = which == 0 ? s.cf0 : which == 1 ? s.nb0 : s.cv0;
+  for (int i = blockIdx.y * kGatherPerBlock + threadIdx.x;
+       i < n && i < (int)(blockIdx.y + 1) * kGatherPerBlock; i += kGatherThreads) {
+    const int x = in[i];
+    out[o + i] = which == 0 ? (x >= 0 ? x + s.f0 : ~(~x + s.f0)) : which == 1 ? x + s.c0 : x + s.v0;
+  }
+}
+
+// carried states: new buffer <- old buffer, per problem with keep_from >= 0
+__global__ void gather_state(const src_mesh *src, const double *old_buf, double *new_buf,
+                             int64_t stride, int planes) {
+  const src_mesh &s = src[blockIdx.x];
+  if (s.keep_from < 0) return;
+  const int n = s.v.num_cells;
+  for (int i = blockIdx.y * kGatherPerBlock + threadIdx.x;
+       i < n && i < (int)(blockIdx.y + 1) * kGatherPerBlock; i += kGatherThreads)
+    for (int pl = 0; pl < planes; ++pl)
+      new_buf[pl * stride + s.c0 + i] = old_buf[pl * stride + s.keep_from + i];
+}
+
+}  // namespace
+
+fvh_status fvh_batch_assign_device(fvh_batch *b, int32_t n,
+                                   const fvh_device_mesh *const *meshes, const double *cfl,
+                                   const double *final_time, const int32_t *keep,
+                                   fvh_stream_t stream) {
+  if (!b || n <= 0 || !meshes || !cfl || !final_time) return FVH_ERR_INVALID_ARGUMENT;
+  if (n > b->max_problems) return FVH_ERR_CAPACITY;
+  const int D = b->dim;
+  std::vector<src_mesh> src(n);
+  int64_t nc = 0, nf = 0, nv = 0, ncf = 0, nnb = 0, ncv = 0;
+  int maxc = 0, maxf = 0, maxv = 0, maxcsr = 0;
+  for (int k = 0; k < n; ++k) {
+    const fvh_device_mesh *m = meshes[k];
+    if (!m || m->view.dim != D || !(cfl[k] > 0)) return FVH_ERR_INVALID_ARGUMENT;
+    if (keep && keep[k] >= b->nproblems) return FVH_ERR_INVALID_ARGUMENT;
+    src_mesh &s = src[k];
+    s.v = m->view;
+    s.c0 = (int32_t)nc; s.f0 = (int32_t)nf; s.v0 = (int32_t)nv;
+    s.cf0 = (int32_t)ncf; s.nb0 = (int32_t)nnb; s.cv0 = (int32_t)ncv;
+    s.ncf = m->nnz_cf; s.nnb = m->nnz_nb; s.ncv = m->nnz_cv;
+    s.keep_from = -1;
+    if (keep && keep[k] >= 0) {
+      const int o = keep[k];
+      if (b->first_cell[o + 1] - b->first_cell[o] != m->view.num_cells) return FVH_ERR_INVALID_ARGUMENT;
+      s.keep_from = b->first_cell[o];
+    }
+    nc += m->view.num_cells; nf += m->view.num_faces; nv += m->view.num_vertices;
+    ncf += m->nnz_cf; nnb += m->nnz_nb; ncv += m->nnz_cv;
+    maxc = std::max(maxc, m->view.num_cells);
+    maxf = std::max(maxf, m->view.num_faces);
+    maxv = std::max(maxv, m->view.num_vertices);
+    maxcsr = std::max({maxcsr, m->nnz_cf, m->nnz_nb, m->nnz_cv});
+  }
+  if (nc > b->max_cells || nf > b->max_faces || nv > b->max_vertices || ncf > b->max_cf ||
+      nnb > b->max_nb || ncv > b->max_cv)
+    return FVH_ERR_CAPACITY;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  std::vector<double> times(n, 0.0);
+  if (keep && b->nproblems > 0) {
+    e = cudaMemcpyAsync(b->h_t, b->t, sizeof(double) * b->nproblems, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (int k = 0; k < n; ++k)
+      if (keep[k] >= 0) times[k] = b->h_t[keep[k]];
+  }
+  // destination view
+  fvh_mesh_view &v = b->view;
+  std::memset(&v, 0, sizeof(v));
+  v.dim = D;
+  v.num_cells = (int32_t)nc;
+  v.num_faces = (int32_t)nf;
+  v.num_vertices = (int32_t)nv;
+  v.face_cells = b->face_cells;
+  v.cell_face_offsets = b->cf_off;
+  v.cell_faces = b->cf;
+  v.cell_nbr_offsets = b->nb_off;
+  v.cell_nbrs = b->nb;
+  v.cell_vertex_offsets = b->cv_off;
+  v.cell_vertices = b->cv;
+  double *g = b->geo;
+  for (int d = 0; d < D; ++d, g += b->max_cells) v.cell_centroid[d] = g;
+  v.cell_volume = g;
+  g += b->max_cells;
+  for (int d = 0; d < D; ++d, g += b->max_faces) v.face_centroid[d] = g;
+  for (int d = 0; d < D; ++d, g += b->max_faces) v.face_normal[d] = g;
+  v.face_area = g;
+  g += b->max_faces;
+  for (int d = 0; d < D; ++d, g += b->max_vertices) v.vertex_coord[d] = g;
+  // descriptors (device copy), problem tables
+  src_mesh *d_src = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_src, sizeof(src_mesh) * n, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_src, src.data(), sizeof(src_mesh) * n, cudaMemcpyHostToDevice, st);
+  std::vector<int32_t> first(n + 1);
+  for (int k = 0; k < n; ++k) first[k] = src[k].c0;
+  first[n] = (int32_t)nc;
+  const int32_t tails[3] = {(int32_t)ncf, (int32_t)nnb, (int32_t)ncv};
+  int32_t *tail_dst[3] = {b->cf_off + nc, b->nb_off + nc, b->cv_off + nc};
+  for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+    e = cudaMemcpyAsync(tail_dst[q], &tails[q], sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_first_cell, first.data(), sizeof(int32_t) * (n + 1),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->cfl, cfl, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->tf, final_time, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->t, times.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dtinv_bits, 0, sizeof(unsigned) * n, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->status, 0xff, sizeof(fvh_device_status) * n, st);
+  const int nxt = 1 - b->cur;
+  if (e == cudaSuccess) {
+    auto chunks = [](int m) { return std::max(1, (m + kGatherPerBlock - 1) / kGatherPerBlock); };
+    gather_cells<<<dim3(n, chunks(maxc)), kGatherThreads, 0, st>>>(d_src, v, b->cell_problem, D);
+    gather_faces<<<dim3(n, chunks(maxf)), kGatherThreads, 0, st>>>(d_src, v, D);
+    gather_vertices<<<dim3(n, chunks(maxv)), kGatherThreads, 0, st>>>(d_src, v, D);
+    for (int which = 0; which < 3; ++which)
+      gather_csr<<<dim3(n, chunks(maxcsr)), kGatherThreads, 0, st>>>(d_src, v, which);
+    gather_state<<<dim3(n, chunks(maxc)), kGatherThreads, 0, st>>>(
+        d_src, b->state_buf[b->cur], b->state_buf[nxt], b->max_cells, 5 + D);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = fvh::mixed::setup_geometry(b->ws, v, st);
+  if (d_src) cudaFreeAsync(d_src, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return from_cuda(e);
   b->cur = nxt;
   set_state_view(b);

@@ -101,10 +101,6 @@ struct fvh_solver {
   fvh_state_view graph_state{};
 };
 
-struct fvh_device_mesh {
-  fvh_mesh_view view{};
-  std::vector<void *> allocs;
-};
 
 struct fvh_device_state {
   fvh_state_view view{};
@@ -546,6 +542,9 @@ fvh_status fvh_device_mesh_create(const fvh_host_mesh *m, fvh_device_mesh **out)
     return static_cast<const double *>(up(v.data(), v.size() * sizeof(double)));
   };
   fvh_mesh_view &o = dm->view;
+  dm->nnz_cf = (int32_t)m->cf.size();
+  dm->nnz_nb = (int32_t)m->nb.size();
+  dm->nnz_cv = (int32_t)m->cv.size();
   o.dim = m->dim;
   o.num_cells = m->nc;
   o.num_faces = m->nf;

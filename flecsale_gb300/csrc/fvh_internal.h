@@ -19,6 +19,13 @@ struct fvh_host_mesh {
   std::vector<double> vc[3];                // vertex coordinates
 };
 
+// Device copy of a host mesh (fvh_device_mesh_create).
+struct fvh_device_mesh {
+  fvh_mesh_view view{};
+  int32_t nnz_cf = 0, nnz_nb = 0, nnz_cv = 0;  // CSR storage lengths
+  std::vector<void *> allocs;
+};
+
 namespace fvh {
 fvh_status build_topology_and_geometry(fvh_host_mesh &m);
 double uniform01(uint64_t seed, uint64_t counter);

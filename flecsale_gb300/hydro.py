@@ -268,11 +268,18 @@ class HostMesh:
     def num_vertices(self) -> int:
         return self.view.num_vertices
 
+    def _view(self, ptr, n, ctype) -> np.ndarray:
+        # the ctypes array is the numpy base and holds a reference to the mesh,
+        # so views outlive neither the arrays nor the mesh
+        buf = (ctype * max(n, 1)).from_address(C.cast(ptr, C.c_void_p).value)
+        buf._owner = self
+        return np.ctypeslib.as_array(buf)[:n]
+
     def _i(self, ptr, n) -> np.ndarray:
-        return np.ctypeslib.as_array(ptr, shape=(n,))
+        return self._view(ptr, n, C.c_int32)
 
     def _d(self, ptr, n) -> np.ndarray:
-        return np.ctypeslib.as_array(ptr, shape=(n,))
+        return self._view(ptr, n, C.c_double)
 
     def arrays(self) -> dict:
         """numpy views (no copies) of every mesh array."""
@@ -547,3 +554,66 @@ class Batch:
             self._h = None
 
     __del__ = close
+
+
+def _declare_io(L: C.CDLL) -> None:
+    vp = C.c_void_p
+    for name, res, args in [
+        ("fvh_host_mesh_read_exodus", C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        ("fvh_dump_write", C.c_int, [C.c_char_p, vp, _dp, C.c_double, C.c_int64]),
+        ("fvh_host_state_from_dvp", C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                               _dp, _dp, _dp, _dp]),
+    ]:
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = res, args
+
+
+def read_exodus(path: str) -> HostMesh:
+    """Mesh from an Exodus II file (netCDF classic / 64-bit offset)."""
+    _declare_io(lib())
+    h = C.c_void_p()
+    check(lib().fvh_host_mesh_read_exodus(path.encode(), C.byref(h)), f"read_exodus({path})")
+    return HostMesh(h)
+
+
+def write_dump(path: str, mesh: HostMesh, planes: np.ndarray, soln_time: float,
+               iterations: int) -> None:
+    """Regression dump in the reference's format (apps/hydro/tasks.h:771-849)."""
+    _declare_io(lib())
+    planes = np.ascontiguousarray(planes[:5 + mesh.dim], np.float64)
+    check(lib().fvh_dump_write(path.encode(), mesh._h, _dptr(planes), soln_time, iterations),
+          "fvh_dump_write")
+
+
+def state_from_dvp(dim: int, density, velocity, pressure, gamma: float = 1.4,
+                   cv: float = 1.0) -> np.ndarray:
+    """State planes (d, v..., e, p, T, a) from density, velocity [dim][n] and pressure."""
+    _declare_io(lib())
+    d = np.ascontiguousarray(density, np.float64)
+    v = np.ascontiguousarray(velocity, np.float64).reshape(dim, -1)
+    p = np.ascontiguousarray(pressure, np.float64)
+    out = np.empty((5 + dim, d.size), np.float64)
+    check(lib().fvh_host_state_from_dvp(dim, d.size, gamma, cv, _dptr(d), _dptr(v), _dptr(p),
+                                        _dptr(out)), "fvh_host_state_from_dvp")
+    return out
+
+
+def _declare_batch_device(L: C.CDLL) -> None:
+    fn = L.fvh_batch_assign_device
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), _dp, _dp, C.POINTER(C.c_int32),
+                   C.c_void_p]
+
+
+def batch_assign_device(batch: "Batch", dmeshes, cfl, final_time, keep=None, stream=None) -> None:
+    """fvh_batch_assign_device: problems already resident in device memory
+    (DeviceMesh) are concatenated on the device."""
+    _declare_batch_device(lib())
+    n = len(dmeshes)
+    arr = (C.c_void_p * n)(*[m._h for m in dmeshes])
+    cf = np.ascontiguousarray(np.broadcast_to(np.asarray(cfl, np.float64), (n,)))
+    tf = np.ascontiguousarray(np.broadcast_to(np.asarray(final_time, np.float64), (n,)))
+    kp = None if keep is None else (C.c_int32 * n)(*keep)
+    check(lib().fvh_batch_assign_device(batch._h, n, arr, _dptr(cf), _dptr(tf), kp,
+                                        stream_handle(stream)), "fvh_batch_assign_device")
+    batch.meshes = list(dmeshes)

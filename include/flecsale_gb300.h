@@ -320,6 +320,29 @@ fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
 
 void fvh_host_mesh_destroy(fvh_host_mesh *m);
 
+/* Read an Exodus II mesh file in the netCDF classic (CDF-1) or 64-bit-offset
+ * (CDF-2) encoding: all element blocks connect1..N (QUAD4/SHELL4 as 2D
+ * polygons, HEX8, TETRA4), coordinates coordx/coordy[/coordz] or coord.
+ * Cell and vertex ids follow the file.  netCDF-4/HDF5 files give
+ * FVH_ERR_UNSUPPORTED.  Replaces the flecsi-sp Exodus reader behind the
+ * reference's "-m mesh" argument (apps/common/arguments.h:44-52). */
+fvh_status fvh_host_mesh_read_exodus(const char *path, fvh_host_mesh **out);
+
+/* Write the regression dump of apps/hydro/tasks.h:771-849 (precision 14,
+ * scientific; cells then vertices) for host state planes
+ * (d, v[0..dim), e, p, T, a). */
+fvh_status fvh_dump_write(const char *path, const fvh_host_mesh *m,
+                          const double *host_planes, double soln_time,
+                          int64_t iterations);
+
+/* EOS closure of caller-provided density, velocity planes [dim][n] and
+ * pressure (update_state_from_pressure, euler_eqns.h:333-350) into state
+ * planes d, v..., e, p, T, a: the second half of initial_conditions
+ * (apps/hydro/tasks.h:58-66). */
+fvh_status fvh_host_state_from_dvp(int32_t dim, int32_t n, double gamma, double cv,
+                                   const double *density, const double *velocity,
+                                   const double *pressure, double *host_planes);
+
 /* Concatenate meshes of one dimension into one block-diagonal mesh: cells,
  * faces and vertices of mesh k follow those of meshes 0..k-1, with all indices
  * shifted; no connectivity is added between meshes. */
@@ -415,6 +438,15 @@ void fvh_batch_destroy(fvh_batch *b);
 fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const *meshes,
                             const double *cfl, const double *final_time,
                             const int32_t *keep, fvh_stream_t stream);
+
+/* Same as fvh_batch_assign for meshes already in device memory
+ * (fvh_device_mesh_create): the concatenation runs on the device, so changing
+ * the set of problems costs no host work or host-to-device traffic for the
+ * problems that stay. */
+fvh_status fvh_batch_assign_device(fvh_batch *b, int32_t n,
+                                   const fvh_device_mesh *const *meshes,
+                                   const double *cfl, const double *final_time,
+                                   const int32_t *keep, fvh_stream_t stream);
 
 /* Host planes (d, v[0..dim), e, p, T, a; one plane per field, problem cells)
  * in and out of problem k; set_state also sets its solution time.  Both
