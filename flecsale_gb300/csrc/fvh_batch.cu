@@ -692,9 +692,7 @@ fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cac
                             sizeof(fvh_device_status) * P, cudaMemcpyDeviceToDevice, st);
     };
     copy_state(true);
-    const fvh::mixed::launch_shape cands[] = {{128, 1, 0}, {256, 1, 0}, {128, 2, 0},
-                                              {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
-                                              {128, 2, 1}};
+    const auto &cands = fvh::mixed::kShapes;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -96,6 +96,7 @@ struct fvh_solver {
   double *host_scalars = nullptr;  // pinned: soln time
   fvh_device_status *host_status = nullptr;
   fvh::mixed::workspace *mixed = nullptr;
+  fvh::mixed::launch_shape shape;  // mixed form's cell-kernel launch shape
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
   fvh_state_view graph_state{};
@@ -313,7 +314,7 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   double *t = s->scalars, *dt = s->scalars + 1, *partial = s->scalars + 2;
   if (p.precision == FVH_PRECISION_MIXED)
     return from_cuda(fvh::mixed::step(s->mixed, m, p, *state, t, dt, partial,
-                                      dt_blocks(m.num_cells), s->status, st, mark));
+                                      dt_blocks(m.num_cells), s->status, st, mark, s->shape));
   const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
   const int nb = dt_blocks(m.num_cells);
   fvh_status r = from_cuda(
@@ -336,9 +337,120 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   return r;
 }
 
+fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
+                                int32_t schedule) {
+  if (!s || (block != 128 && block != 256) || cells_per_thread < 1 || cells_per_thread > 8 ||
+      (schedule != 0 && schedule != 1))
+    return FVH_ERR_INVALID_ARGUMENT;
+  s->shape.block = block;
+  s->shape.cells_per_thread = cells_per_thread;
+  s->shape.schedule = schedule;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return FVH_OK;
+}
+
+fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32_t trial_steps,
+                               int32_t *block, int32_t *cells_per_thread, int32_t *schedule,
+                               double *best_ms_per_step, fvh_stream_t stream) {
+  if (!s || !state_ok(state, s->mesh.dim) || trial_steps <= 0) return FVH_ERR_INVALID_ARGUMENT;
+  if (s->params.precision != FVH_PRECISION_MIXED) {  // the FP64 path has one shape
+    if (block) *block = 128;
+    if (cells_per_thread) *cells_per_thread = 1;
+    if (schedule) *schedule = 0;
+    if (best_ms_per_step) *best_ms_per_step = -1;
+    return FVH_OK;
+  }
+  cudaStream_t st = cs(stream);
+  const int D = s->mesh.dim;
+  const size_t nc = s->mesh.num_cells;
+  // trials run on a scratch copy of the state; the caller's state, solution
+  // time and status word are left as they were
+  double *scratch = nullptr, *saved_t = nullptr;
+  cudaError_t e = cudaMalloc(&scratch, sizeof(double) * (5 + D) * nc);
+  if (e == cudaSuccess) e = cudaMalloc(&saved_t, sizeof(double) + sizeof(fvh_device_status));
+  if (e != cudaSuccess) {
+    cudaFree(scratch);
+    return from_cuda(e);
+  }
+  double *planes_src[9], *planes_dst[9];
+  fvh_state_view tmp{};
+  {
+    int k = 0;
+    planes_src[k++] = state->density;
+    for (int d = 0; d < D; ++d) planes_src[k++] = state->velocity[d];
+    planes_src[k++] = state->internal_energy;
+    planes_src[k++] = state->pressure;
+    planes_src[k++] = state->temperature;
+    planes_src[k++] = state->sound_speed;
+    for (int q = 0; q < 5 + D; ++q) planes_dst[q] = scratch + q * nc;
+    k = 0;
+    tmp.density = planes_dst[k++];
+    for (int d = 0; d < D; ++d) tmp.velocity[d] = planes_dst[k++];
+    tmp.internal_energy = planes_dst[k++];
+    tmp.pressure = planes_dst[k++];
+    tmp.temperature = planes_dst[k++];
+    tmp.sound_speed = planes_dst[k++];
+  }
+  e = cudaMemcpyAsync(saved_t, s->scalars, sizeof(double), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(saved_t + 1, s->status, sizeof(fvh_device_status), cudaMemcpyDeviceToDevice, st);
+  auto refresh = [&]() {
+    for (int q = 0; q < 5 + D && e == cudaSuccess; ++q)
+      e = cudaMemcpyAsync(planes_dst[q], planes_src[q], sizeof(double) * nc,
+                          cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->scalars, saved_t, sizeof(double), cudaMemcpyDeviceToDevice, st);
+  };
+  const fvh::mixed::launch_shape keep = s->shape;
+  fvh::mixed::launch_shape best = keep;
+  double best_ms = -1;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (const auto &c : fvh::mixed::kShapes) {
+    if (e != cudaSuccess) break;
+    fvh_solver_set_shape(s, c.block, c.cells_per_thread, c.schedule);
+    refresh();
+    fvh_status r = FVH_OK;
+    for (int k = 0; k < trial_steps && r == FVH_OK; ++k) r = fvh_solver_step(s, &tmp, stream);
+    refresh();
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < trial_steps && r == FVH_OK; ++k) r = fvh_solver_step(s, &tmp, stream);
+    cudaEventRecord(e1, st);
+    if (r == FVH_OK) e = cudaEventSynchronize(e1);
+    if (r != FVH_OK || e != cudaSuccess) continue;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best_ms < 0 || ms / trial_steps < best_ms) {
+      best_ms = ms / trial_steps;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->scalars, saved_t, sizeof(double), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->status, saved_t + 1, sizeof(fvh_device_status), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(scratch);
+  cudaFree(saved_t);
+  fvh_solver_set_shape(s, best.block, best.cells_per_thread, best.schedule);
+  if (e != cudaSuccess) return from_cuda(e);
+  if (block) *block = best.block;
+  if (cells_per_thread) *cells_per_thread = best.cells_per_thread;
+  if (schedule) *schedule = best.schedule;
+  if (best_ms_per_step) *best_ms_per_step = best_ms;
+  return FVH_OK;
+}
+
 int32_t fvh_solver_launches_per_step(const fvh_solver *s) {
   if (!s) return 0;
-  if (s->params.precision == FVH_PRECISION_MIXED) return fvh::mixed::launches_per_step(s->params);
+  if (s->params.precision == FVH_PRECISION_MIXED)
+    return fvh::mixed::launches_per_step(s->params, s->shape);
   // dt (partial + final) + per stage: gradients (or D*(D+4) memsets), fluxes, update
   const int D = s->mesh.dim;
   const int grad = s->params.order == 1 ? D * (D + 4) : 1;

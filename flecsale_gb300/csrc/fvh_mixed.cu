@@ -59,8 +59,8 @@ struct workspace {
   float4 *fgeo = nullptr;    // face normal + area
   float4 *fdx = nullptr;     // face centroid offsets from both cells
   float4 *fflux = nullptr;   // face schedule: area-scaled face fluxes
-  double *inv_vol = nullptr; // 1/V (FP64)
-  float *inv_vol32 = nullptr; // 1/V (FP32, for the CFL estimate)
+  float *inv_vol32 = nullptr;  // 1/V rounded to FP32 (CFL estimate; update, high part)
+  float *inv_vol_lo = nullptr; // 1/V - inv_vol32, rounded to FP32 (update, low part)
 };
 
 // Load pack fields: slots (d, v0, v1, [v2,] p, e, a) in the AoS order
@@ -165,6 +165,48 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
   lo = __fadd_rn(lo, err);
 }
 
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two FP32
+// numbers (about 48 significant bits).  Built from Knuth's two-sum, Dekker's
+// fast two-sum and the FMA two-product; every operation is an explicit
+// round-to-nearest intrinsic so the compiler neither contracts nor
+// reassociates them.  It runs on the FP32 pipe, 64x wider than the FP64 pipe.
+struct df {
+  float hi, lo;
+};
+__device__ __forceinline__ df df_fast2(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+  const float s = __fadd_rn(x.hi, y.hi);
+  const float bb = __fsub_rn(s, x.hi);
+  const float err = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+  return df_fast2(s, __fadd_rn(err, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, {-y.hi, -y.lo}); }
+__device__ __forceinline__ df df_mul(df x, df y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast2(p, e);
+}
+__device__ __forceinline__ df df_half(df x) { return {0.5f * x.hi, 0.5f * x.lo}; }
+// x / y given r = RN(1/y.hi): quotient estimate, its double-float residual and
+// one correction term
+__device__ __forceinline__ df df_div(df x, df y, float r) {
+  const float q1 = __fmul_rn(x.hi, r);
+  const df res = df_sub(x, df_mul(y, {q1, 0.f}));
+  return df_fast2(q1, __fmul_rn(res.hi, r));
+}
+// FP64 -> double-float: one FP64 subtraction, conversions on the integer pipe
+__device__ __forceinline__ df df_from(double x) {
+  const float h = d2f(x);
+  return {h, d2f(x - f2d(h))};
+}
+// x + d in FP64 (two FP64 additions; x keeps all of its bits)
+__device__ __forceinline__ double add_df(double x, df d) { return (x + f2d(d.hi)) + f2d(d.lo); }
+
 // ---------------------------------------------------------------------------
 // setup: FP32 geometry derived once from the FP64 mesh
 // ---------------------------------------------------------------------------
@@ -185,8 +227,9 @@ __global__ void setup_cells(const fvh_mesh_view m, workspace w) {
     w.ccen[2 * (size_t)c] = make_float4(hi[0], hi[1], hi[D - 1], 0.f);
     w.ccen[2 * (size_t)c + 1] = make_float4(lo[0], lo[1], lo[D - 1], 0.f);
   }
-  w.inv_vol[c] = 1.0 / m.cell_volume[c];
-  w.inv_vol32[c] = (float)(1.0 / m.cell_volume[c]);
+  const float2 iv = split(1.0 / m.cell_volume[c]);
+  w.inv_vol32[c] = iv.x;
+  w.inv_vol_lo[c] = iv.y;
 }
 
 template <int D>
@@ -537,11 +580,13 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 // reconstruct the state of cell c at offset dx (x_f - x_c) from pack + grads
 template <int D, bool SECOND>
 __device__ __forceinline__ prim<float, D> recon(const workspace &w, const float4 *pk, int c,
-                                                const float *dx, bool swap) {
-  prim<float, D> u = load_pack<D>(pk, c);
+                                                const float *dx, bool swap);
+
+// reconstruction of cell values u (pack) with gradients g at offset dx
+template <int D, bool SECOND>
+__device__ __forceinline__ prim<float, D> recon_from(prim<float, D> u, const float *g,
+                                                     const float *dx, bool swap) {
   if (SECOND) {
-    float g[4 * layout<D>::GRAD4];
-    load_grads<D>(w.grads, c, g);
     // gradient rows: 0 d, 1..D v, D+1 e, D+2 p, D+3 a
     const int ge = swap ? D + 2 : D + 1;  // row added to the energy slot
     const int gp = swap ? D + 1 : D + 2;  // row added to the pressure slot
@@ -556,6 +601,14 @@ __device__ __forceinline__ prim<float, D> recon(const workspace &w, const float4
     }
   }
   return u;
+}
+
+template <int D, bool SECOND>
+__device__ __forceinline__ prim<float, D> recon(const workspace &w, const float4 *pk, int c,
+                                                const float *dx, bool swap) {
+  float g[4 * layout<D>::GRAD4];
+  if (SECOND) load_grads<D>(w.grads, c, g);
+  return recon_from<D, SECOND>(load_pack<D>(pk, c), g, dx, swap);
 }
 
 // Area-scaled flux of face f in its own orientation (cells(f)[0] -> [1]),
@@ -590,47 +643,78 @@ __device__ __forceinline__ void face_flux_area(const fvh_mesh_view &m, const wor
   for (int k = 0; k < D + 2; ++k) F[k] = __fmul_rn(F[k], area);
 }
 
-// Conservative FP64 update of cell c from its compensated face sums
-// (update_state_from_flux + update_state_from_energy), writes the FP64 state
-// and the next pack record.
+// Constants of the conservative update.
+struct update_consts {
+  df gm1;        // gamma - 1
+  float ggm1;    // gamma (gamma - 1), for the FP32 sound speed
+  float factor;  // fraction of dt this stage advances (0.5)
+  double inv_cv; // 1 / cv
+  int unit_cv;   // cv == 1: T = e exactly
+};
+
+// x < 0 (not -0, not +NaN) from the bits, off the FP64 pipe
+__device__ __forceinline__ bool negative(double x) {
+  return (unsigned long long)__double_as_longlong(x) > 0x8000000000000000ull;
+}
+
+// Conservative update of cell c from its compensated face sums
+// (update_state_from_flux + update_state_from_energy, tasks.h:589-659).  The
+// cell's FP64 state enters and leaves in FP64; the increments are carried in
+// double-float:
+//   rho' = rho + dU0,   v' = v + (dUm - v dU0) / rho',
+//   e'   = e + (dUE - (e + |v|^2/2) dU0) / rho' - v.dv - |dv|^2/2
+// with dU = (face sum) dt / V.  Each new FP64 value is its old value plus one
+// double-float increment, so rho'(e' + |v'|^2/2) is the old total energy plus
+// dUE to about 2^-48 relative, and the FP64 pipe does D + 2 splits and
+// 2D + 5 additions per cell.  Writes the FP64 state and the next pack record.
 template <int D>
 __device__ __forceinline__ void cell_update(const fvh_state_view &s, const workspace &w,
                                             float4 *__restrict__ pk_out, const problem_map &pm,
-                                            int c, int pr, double delta_t, const float *shi,
-                                            const float *slo, double gm1, float ggm1,
-                                            double inv_cv) {
-  double du[D + 2];
+                                            int c, int pr, df dts, const float *shi,
+                                            const float *slo, const update_consts &k) {
+  const df scale = df_mul(dts, {w.inv_vol32[c], w.inv_vol_lo[c]});
+  df du[D + 2];
 #pragma unroll
-  for (int k = 0; k < D + 2; ++k) du[k] = f2d(shi[k]) + f2d(slo[k]);
-  const double scale = delta_t * w.inv_vol[c];
+  for (int q = 0; q < D + 2; ++q) du[q] = df_mul({shi[q], slo[q]}, scale);
+  const double den0 = s.density[c], e0 = s.internal_energy[c];
   double vel[D];
-#pragma unroll
-  for (int i = 0; i < D; ++i) vel[i] = s.velocity[i][c];
-  const double den0 = s.density[c];
-  const double mass = den0 + du[0] * scale;
-  double ke = 0.0;
-#pragma unroll
-  for (int i = 0; i < D; ++i) ke += vel[i] * vel[i];
-  const double ener = den0 * (s.internal_energy[c] + 0.5 * ke) + du[D + 1] * scale;
-  // 1/mass: FP32 estimate refined by one Newton step in FP64
-  double inv_mass = f2d(__frcp_rn(d2f(mass)));
-  inv_mass = inv_mass * (2.0 - mass * inv_mass);
-  ke = 0.0;
+  df v0[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    vel[i] = (den0 * vel[i] + du[1 + i] * scale) * inv_mass;
-    ke += vel[i] * vel[i];
+    vel[i] = s.velocity[i][c];
+    v0[i] = df_from(vel[i]);
   }
-  const double e = ener * inv_mass - 0.5 * ke;
-  const double p = gm1 * mass * e;
+  const df rho = df_add(df_from(den0), du[0]);
+  const float r = __frcp_rn(rho.hi);
+  df k0 = {0.f, 0.f}, dv[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    k0 = df_add(k0, df_mul(v0[i], v0[i]));
+    dv[i] = df_div(df_sub(du[1 + i], df_mul(v0[i], du[0])), rho, r);
+  }
+  const df e0d = df_from(e0);
+  df de = df_div(df_sub(du[D + 1], df_mul(df_add(e0d, df_half(k0)), du[0])), rho, r);
+  df vdv = {0.f, 0.f}, dv2 = {0.f, 0.f};
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    vdv = df_add(vdv, df_mul(v0[i], dv[i]));
+    dv2 = df_add(dv2, df_mul(dv[i], dv[i]));
+  }
+  de = df_sub(de, df_add(vdv, df_half(dv2)));
+  const double mass = add_df(den0, du[0]);
+#pragma unroll
+  for (int i = 0; i < D; ++i) vel[i] = add_df(vel[i], dv[i]);
+  const double e = add_df(e0, de);
+  const df pd = df_mul(k.gm1, df_mul(rho, df_add(e0d, de)));
+  const double p = f2d(pd.hi) + f2d(pd.lo);
   const float ef = d2f(e);
-  const float a = sqrtf(ggm1 * ef);
+  const float a = sqrtf(k.ggm1 * ef);
   s.density[c] = mass;
 #pragma unroll
   for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
   s.internal_energy[c] = e;
   s.pressure[c] = p;
-  s.temperature[c] = e * inv_cv;
+  s.temperature[c] = k.unit_cv ? e : e * k.inv_cv;
   s.sound_speed[c] = f2d(a);
   if (pk_out) {
     float vf[D];
@@ -638,25 +722,46 @@ __device__ __forceinline__ void cell_update(const fvh_state_view &s, const works
     for (int i = 0; i < D; ++i) vf[i] = d2f(vel[i]);
     store_pack<D>(pk_out, c, d2f(mass), vf, d2f(p), ef, a);
   }
-  if (e < 0 || mass < 0) atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
+  if (negative(e) || negative(mass))
+    atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
 }
+
+// Per-thread cache of the stage's dt for the problem of the current cell; the
+// problem's solution time is advanced by its first cell.  Returns false for a
+// finished problem (dt == 0), whose state is left untouched.
+struct stage_dt {
+  int pr = -1;
+  bool live = false;
+  df dts;
+  __device__ __forceinline__ bool at(const problem_map &pm, int c, int cpr, float factor) {
+    if (cpr != pr) {
+      pr = cpr;
+      const double dt = pm.dt[pr];
+      live = (__double_as_longlong(dt) << 1) != 0;
+      dts = df_from(dt);
+      dts.hi *= factor;  // factor is a power of two: exact
+      dts.lo *= factor;
+    }
+    if (c == (pm.cell_problem ? pm.first_cell[pr] : 0))
+      pm.t[pr] = pm.t[pr] + pm.dt[pr] * (double)factor;
+    return live;
+  }
+};
 
 // Cell-centric schedule: each cell evaluates the fluxes of its own faces.
 template <int D, int KIND, bool SECOND, int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                    const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out,
-                   const problem_map pm, double factor, double gm1, float ggm1, double inv_cv,
-                   int swap, int outflow) {
+                   const problem_map pm, const update_consts k, int swap, int outflow) {
   // Reads only pk_in (all cells) and the cell's own FP64 state; writes the
   // cell's FP64 state and its pk_out record (null after the corrector).
+  stage_dt sdt;
   for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    const double delta_t = pm.dt[pr] * factor;
-    if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
-    if (delta_t == 0.0) continue;  // finished problem: leave its state untouched
+    if (!sdt.at(pm, c, pr, k.factor)) continue;
     // face sums in FP32 with error-free two-sum compensation (hi + lo carries
-    // about 48 bits), one FP64 add per component afterwards
+    // about 48 bits)
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
@@ -669,7 +774,7 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D>(s, w, pk_out, pm, c, pr, delta_t, shi, slo, gm1, ggm1, inv_cv);
+    cell_update<D>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, k);
   }
 }
 
@@ -694,14 +799,13 @@ face_flux_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 template <int D, int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
-                     float4 *__restrict__ pk_out, const problem_map pm, double factor,
-                     double gm1, float ggm1, double inv_cv) {
+                     float4 *__restrict__ pk_out, const problem_map pm,
+                     const update_consts k) {
   constexpr int F4 = layout<D>::FLUX4;
+  stage_dt sdt;
   for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    const double delta_t = pm.dt[pr] * factor;
-    if (c == (pm.cell_problem ? pm.first_cell[pr] : 0)) pm.t[pr] = pm.t[pr] + delta_t;
-    if (delta_t == 0.0) continue;  // finished problem: leave its state untouched
+    if (!sdt.at(pm, c, pr, k.factor)) continue;
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
@@ -721,7 +825,7 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D>(s, w, pk_out, pm, c, pr, delta_t, shi, slo, gm1, ggm1, inv_cv);
+    cell_update<D>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, k);
   }
 }
 
@@ -733,7 +837,7 @@ static size_t bytes_for(int nc, int nf, int nv) {
   using L = layout<D>;
   return sizeof(float4) * ((size_t)nc * (2 * L::PACK4 + L::GRAD4 + L::CEN4) + (size_t)nv * L::CEN4 +
                            (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4)) +
-         sizeof(double) * (size_t)nc + sizeof(float) * (size_t)nc + 256 * 9;
+         2 * sizeof(float) * (size_t)nc + 256 * 9;
 }
 
 template <int D>
@@ -753,8 +857,8 @@ static void carve(workspace *w) {
   w->fgeo = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FGEO4));
   w->fdx = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FDX4));
   w->fflux = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FLUX4));
-  w->inv_vol = reinterpret_cast<double *>(take(sizeof(double) * (size_t)w->nc));
   w->inv_vol32 = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
+  w->inv_vol_lo = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
 }
 
 template <int D>
@@ -834,18 +938,24 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
       gradients_kernel<D, true, BS><<<nb, BS, 0, st>>>(m, *w, pk_in);
     mark("gradients");
   }
-  const double gm1 = p.gamma - 1.0, inv_cv = 1.0 / p.cv;
-  const float ggm1 = (float)(p.gamma * (p.gamma - 1.0));
+  update_consts k;
+  const double gm1 = p.gamma - 1.0;
+  k.gm1.hi = (float)gm1;
+  k.gm1.lo = (float)(gm1 - (double)k.gm1.hi);
+  k.ggm1 = (float)(p.gamma * (p.gamma - 1.0));
+  k.factor = 0.5f;
+  k.inv_cv = 1.0 / p.cv;
+  k.unit_cv = p.cv == 1.0;
   if (schedule == 1) {
     const int nbf = (int)((m.num_faces + per - 1) / per);
     face_flux_kernel<D, KIND, SECOND, BS><<<nbf, BS, 0, st>>>(m, *w, pk_in, p.recon_swap_ep,
                                                                p.boundary);
     mark("face_flux");
-    gather_update_kernel<D, BS><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, 0.5, gm1, ggm1, inv_cv);
+    gather_update_kernel<D, BS><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
     mark("gather_update");
   } else {
     flux_update_kernel<D, KIND, SECOND, BS><<<nb, BS, 0, st>>>(
-        m, s, *w, pk_in, pk_out, pm, 0.5, gm1, ggm1, inv_cv, p.recon_swap_ep, p.boundary);
+        m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
     mark("flux_update");
   }
 }
@@ -890,7 +1000,7 @@ template <int D>
 static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                           const fvh_state_view &s, double *t, double *dt, double *partial,
                           int dt_blocks, fvh_device_status *status, cudaStream_t st,
-                          const launch_mark &mark) {
+                          const launch_mark &mark, const launch_shape &shape) {
   pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial);
   mark("pack_dt");
   dt_final_kernel<<<1, kDtThreads, 0, st>>>(partial, dt_blocks, p, t, dt, status);
@@ -899,16 +1009,17 @@ static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params
   pm.dt = dt;
   pm.t = t;
   pm.status = status;
-  launch_stages<D>(w, m, p, s, pm, launch_shape(), st, mark);
+  launch_stages<D>(w, m, p, s, pm, shape, st, mark);
   return cudaGetLastError();
 }
 
 cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                  const fvh_state_view &s, double *soln_time, double *dt, double *partial,
                  int dt_blocks, fvh_device_status *status, cudaStream_t st,
-                 const launch_mark &mark) {
-  return m.dim == 2 ? step_d<2>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark)
-                    : step_d<3>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark);
+                 const launch_mark &mark, const launch_shape &shape) {
+  return m.dim == 2
+             ? step_d<2>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape)
+             : step_d<3>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape);
 }
 
 template <int D>

@@ -29,14 +29,31 @@ struct launch_mark {
   }
 };
 
+// Launch shape of the cell kernels (picked by the autotuner).  All shapes give
+// the same results bit for bit.
+struct launch_shape {
+  int block = 128;          // threads per block: 128 or 256
+  int cells_per_thread = 1; // grid = ceil(cells / (block * cells_per_thread)), grid-stride
+  int schedule = 0;         // 0: cell-centric (each cell evaluates its faces' fluxes);
+                            // 1: one flux per face into an array, then a cell gather
+};
+
+// Candidate shapes the autotuners time.
+constexpr int kNumShapes = 7;
+constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2, 0},
+                                              {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
+                                              {128, 2, 1}};
+
 // One full time step (dt + two half-dt stages) on the FP64 state.
 cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                  const fvh_state_view &s, double *soln_time, double *dt,
                  double *partial, int dt_blocks, fvh_device_status *status,
-                 cudaStream_t st, const launch_mark &mark = launch_mark());
+                 cudaStream_t st, const launch_mark &mark = launch_mark(),
+                 const launch_shape &shape = launch_shape());
 
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
+int launches_per_step(const fvh_params &p, const launch_shape &sh);
 
 // Independent problems concatenated into one mesh: problem k owns the cells
 // [first_cell[k], first_cell[k+1]).  All arrays are device memory.
@@ -51,15 +68,6 @@ struct problem_map {
   unsigned *dtinv_bits = nullptr;      // [P] max (a+|v.n|)A/V as FP32 bits; reset each step
   fvh_device_status *status = nullptr; // [P]
 };
-
-// Launch shape of the cell kernels (picked by the autotuner).
-struct launch_shape {
-  int block = 128;          // threads per block: 128 or 256
-  int cells_per_thread = 1; // grid = ceil(cells / (block * cells_per_thread)), grid-stride
-  int schedule = 0;         // 0: cell-centric (each cell evaluates its faces' fluxes);
-                            // 1: one flux per face into an array, then a cell gather
-};
-int launches_per_step(const fvh_params &p, const launch_shape &sh);
 
 // One time step of every problem of the batch (per-problem dt and time).
 cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p,

@@ -135,6 +135,10 @@ def _declare(L: C.CDLL) -> None:
         "fvh_solver_advance_host": (C.c_int, [vp, C.POINTER(StateView), _dp, C.c_int64,
                                               C.POINTER(C.c_double), vp]),
         "fvh_solver_launches_per_step": (C.c_int32, [vp]),
+        "fvh_solver_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
+        "fvh_solver_autotune": (C.c_int, [vp, C.POINTER(StateView), C.c_int32,
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_double), vp]),
         "fvh_evaluate_time_step_noalloc": (C.c_int, [C.POINTER(MeshView), C.POINTER(StateView),
                                                      C.POINTER(Params), vp, vp, vp, vp]),
         "fvh_time_step_noalloc_max_cells": (C.c_int32, []),
@@ -437,6 +441,19 @@ class Solver:
 
     def launches_per_step(self) -> int:
         return lib().fvh_solver_launches_per_step(self._h)
+
+    def set_shape(self, block: int, cells_per_thread: int, schedule: int = 0) -> None:
+        check(lib().fvh_solver_set_shape(self._h, block, cells_per_thread, schedule),
+              "fvh_solver_set_shape")
+
+    def autotune(self, state: DeviceState, trial_steps: int = 5, stream=None) -> dict:
+        """Times each launch shape on a scratch copy of `state`; keeps the fastest."""
+        blk, cpt, sch, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double()
+        check(lib().fvh_solver_autotune(self._h, C.byref(state.view), trial_steps, C.byref(blk),
+                                        C.byref(cpt), C.byref(sch), C.byref(ms),
+                                        stream_handle(stream)), "fvh_solver_autotune")
+        return {"block": blk.value, "cells_per_thread": cpt.value, "schedule": sch.value,
+                "ms_per_step": ms.value}
 
     def profile(self, state: DeviceState, nsteps: int, stream=None) -> dict:
         """{kernel name: (mean ms per launch, launches per step)}."""

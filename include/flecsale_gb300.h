@@ -277,6 +277,22 @@ const fvh_flux_view *fvh_solver_fluxes(fvh_solver *s);
 /* Kernel launches one fvh_solver_step makes (the CUDA graph's node count). */
 int32_t fvh_solver_launches_per_step(const fvh_solver *s);
 
+/* Launch shape of the mixed form's cell kernels: block 128 or 256, cells per
+ * thread 1..8, schedule 0 (each cell evaluates its faces' fluxes) or 1 (one
+ * flux per face into an array, then a cell gather).  Every shape gives the
+ * same results bit for bit.  The FP64 form ignores it.  No reference
+ * counterpart: the reference's tasks have no launch configuration. */
+fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
+                                int32_t schedule);
+
+/* Times each candidate launch shape for trial_steps steps on a scratch copy
+ * of `state` and keeps the fastest; the state, solution time and status word
+ * are left unchanged.  Synchronises; allocates the scratch copy.  No
+ * reference counterpart. */
+fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32_t trial_steps,
+                               int32_t *block, int32_t *cells_per_thread, int32_t *schedule,
+                               double *best_ms_per_step, fvh_stream_t stream);
+
 /* Profiling run: nsteps steps launched kernel by kernel with a CUDA event
  * recorded on the stream after every launch.  For each distinct kernel name
  * (at most max_kernels) returns its static name, its mean duration in

@@ -83,3 +83,48 @@ def test_mixed_deterministic(cuda):
     a, _ = _run(mesh, p, s0, 25)
     b, _ = _run(mesh, p, s0, 25)
     assert np.array_equal(a, b)
+
+
+SHAPES = [(128, 1, 0), (256, 1, 0), (128, 2, 0), (256, 2, 0), (128, 1, 1), (256, 1, 1),
+          (128, 2, 1), (128, 3, 0), (256, 4, 1)]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_solver_shapes_bitwise_equal(cuda, dim):
+    """Every launch shape of the mixed solver gives the same bits; autotuning
+    leaves the state, solution time and status word as they were."""
+    n = (160, 120) if dim == 2 else (20, 18, 16)
+    mesh = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, 0.2, 4)
+    p = H.make_params(dim, flux="hllc", cfl=0.4 if dim == 2 else 0.3, precision="mixed",
+                      boundary="outflow")
+    s0 = H.initial_state("four_quadrant" if dim == 2 else "inner_cube", mesh, p, seed=3)
+    dmesh = H.DeviceMesh(mesh)
+    outs = []
+    for shape in SHAPES:
+        dstate = H.DeviceState(dim, mesh.num_cells)
+        solver = H.Solver(dmesh, p)
+        solver.set_shape(*shape)
+        dstate.upload(s0)
+        solver.reset(0.0)
+        solver.run(dstate, 12)
+        code, t, _ = solver.status()
+        assert code == 0
+        outs.append((dstate.download(), t))
+    for s, t in outs[1:]:
+        assert t == outs[0][1]
+        assert np.array_equal(s, outs[0][0])
+    # autotune then run: same bits as the untuned run
+    dstate = H.DeviceState(dim, mesh.num_cells)
+    solver = H.Solver(dmesh, p)
+    dstate.upload(s0)
+    solver.reset(0.0)
+    best = solver.autotune(dstate, trial_steps=2)
+    assert (best["block"], best["cells_per_thread"], best["schedule"]) in SHAPES
+    assert best["ms_per_step"] > 0
+    assert np.array_equal(dstate.download(), s0)
+    code, t, _ = solver.status()
+    assert code == 0 and t == 0.0
+    solver.run(dstate, 12)
+    assert np.array_equal(dstate.download(), outs[0][0])
+    with pytest.raises(H.FvhError):
+        solver.set_shape(64, 1, 0)
