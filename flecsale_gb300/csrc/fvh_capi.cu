@@ -447,6 +447,13 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
   return FVH_OK;
 }
 
+fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, float *rn32,
+                           double *hi_as_double, fvh_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !hi || !lo || !rn32 || !hi_as_double)))
+    return FVH_ERR_INVALID_ARGUMENT;
+  return from_cuda(fvh::mixed::debug_split(x, n, hi, lo, rn32, hi_as_double, cs(stream)));
+}
+
 int32_t fvh_solver_launches_per_step(const fvh_solver *s) {
   if (!s) return 0;
   if (s->params.precision == FVH_PRECISION_MIXED)

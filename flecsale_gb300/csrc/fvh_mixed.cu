@@ -46,6 +46,10 @@ struct layout {
   static constexpr int FGEO4 = 1;              // normal[D], area
   static constexpr int FDX4 = D == 2 ? 1 : 2;  // x_f - x_c0, x_f - x_c1
   static constexpr int FLUX4 = D == 2 ? 1 : 2; // face flux (D+2 floats, padded)
+  static constexpr int DEL4 = D == 2 ? 2 : 3;  // predictor increments (D+2 double-floats)
+  // ELL width of the vertex-offset table (vertices beyond come from the mesh
+  // CSR): what a quadrilateral / hexahedral cell has
+  static constexpr int W_CV = D == 2 ? 4 : 8;
 };
 
 struct workspace {
@@ -59,16 +63,36 @@ struct workspace {
   float4 *fgeo = nullptr;    // face normal + area
   float4 *fdx = nullptr;     // face centroid offsets from both cells
   float4 *fflux = nullptr;   // face schedule: area-scaled face fluxes
+  float4 *delta = nullptr;   // predictor increments of (d, v.., e) as double-floats
   float *inv_vol32 = nullptr;  // 1/V rounded to FP32 (CFL estimate; update, high part)
   float *inv_vol_lo = nullptr; // 1/V - inv_vol32, rounded to FP32 (update, low part)
+  // Column-major ELL table of the offsets x_v - x_c (FP32) of each cell's
+  // first W_CV vertices, [(k * D + i) * nc + c]: a warp's 32 consecutive cells
+  // read 32 consecutive words, with no dependent index load
+  float *ell_vdx = nullptr;
 };
+
+__device__ __forceinline__ void stg256(float4 *p, float4 a, float4 b) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x),
+               "f"(a.y), "f"(a.z), "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+               : "memory");
+}
+
+// one 32-byte load through the read-only path (sm_100+ 256-bit vector load);
+// p must be 32-byte aligned and not written during the kernel
+__device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
 
 // Load pack fields: slots (d, v0, v1, [v2,] p, e, a) in the AoS order
 //   2D: f4[0] = (d, vx, vy, p)  f4[1] = (e, a, 0, 0)
 //   3D: f4[0] = (d, vx, vy, vz) f4[1] = (p, e, a, 0)
 template <int D>
 __device__ __forceinline__ prim<float, D> load_pack(const float4 *pk, int c) {
-  const float4 a = pk[2 * (size_t)c], b = pk[2 * (size_t)c + 1];
+  float4 a, b;
+  ldg256(pk + 2 * (size_t)c, a, b);
   prim<float, D> w;
   w.d = a.x;
   w.v[0] = a.y;
@@ -102,13 +126,20 @@ __device__ __forceinline__ void store_pack(float4 *pk, int c, float d, const flo
 template <int D>
 __device__ __forceinline__ void load_grads(const float4 *gr, int c, float *g) {
   constexpr int G4 = layout<D>::GRAD4;
+  float4 t[G4];
+  if (G4 % 2 == 0) {  // 32-byte aligned records: 256-bit loads
+#pragma unroll
+    for (int q = 0; q < G4; q += 2) ldg256(gr + (size_t)G4 * c + q, t[q], t[q + 1]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < G4; ++q) t[q] = gr[(size_t)G4 * c + q];
+  }
 #pragma unroll
   for (int q = 0; q < G4; ++q) {
-    const float4 t = gr[(size_t)G4 * c + q];
-    g[4 * q] = t.x;
-    g[4 * q + 1] = t.y;
-    g[4 * q + 2] = t.z;
-    g[4 * q + 3] = t.w;
+    g[4 * q] = t[q].x;
+    g[4 * q + 1] = t[q].y;
+    g[4 * q + 2] = t[q].z;
+    g[4 * q + 3] = t[q].w;
   }
 }
 
@@ -151,7 +182,8 @@ __device__ __forceinline__ float d2f(double x) {
   const unsigned r = lo & 0x1fffffffu;
   const unsigned up = (r > 0x10000000u) | ((r == 0x10000000u) & (m & 1u));
   unsigned f = (((unsigned)e) << 23) + m + up;  // a carry out of m bumps the exponent
-  f = e <= 0 ? 0u : (e >= 255 ? 0x7f800000u : f);
+  const bool nan = (hi & 0x7fffffffu) > 0x7ff00000u || ((hi & 0x7fffffffu) == 0x7ff00000u && lo);
+  f = e <= 0 ? 0u : (e >= 255 ? (nan ? 0x7fc00000u : 0x7f800000u) : f);
   return __uint_as_float(sign | f);
 }
 
@@ -199,10 +231,30 @@ __device__ __forceinline__ df df_div(df x, df y, float r) {
   const df res = df_sub(x, df_mul(y, {q1, 0.f}));
   return df_fast2(q1, __fmul_rn(res.hi, r));
 }
-// FP64 -> double-float: one FP64 subtraction, conversions on the integer pipe
+// FP64 -> double-float (hi, lo) with hi + lo = x to about 2^-48 relative.
+//
+// The split uses integer instructions only.  hi = RN32(x) as in d2f; with
+// x = M 2^(E-1075) (53-bit integer M, biased exponent E), x - hi is exactly
+// n 2^(E-1075) for the signed 29-bit remainder n = (M mod 2^29) - 2^29 [hi
+// rounded up], so lo = RN32(x - hi) is one integer-to-float conversion of n
+// times a power of two written into an exponent field.  |x| below 2^-74 gets
+// lo = 0 (and hi = 0 below 2^-126, as in d2f).
 __device__ __forceinline__ df df_from(double x) {
-  const float h = d2f(x);
-  return {h, d2f(x - f2d(h))};
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int E = (int)((hi >> 20) & 0x7ffu);
+  const int e = E - 896;
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned r = lo & 0x1fffffffu;
+  const unsigned up = (r > 0x10000000u) | ((r == 0x10000000u) & (m & 1u));
+  unsigned f = (((unsigned)e) << 23) + m + up;
+  const bool nan = (hi & 0x7fffffffu) > 0x7ff00000u || ((hi & 0x7fffffffu) == 0x7ff00000u && lo);
+  f = e <= 0 ? 0u : (e >= 255 ? (nan ? 0x7fc00000u : 0x7f800000u) : f);
+  const int n = (int)r - (int)(up << 29);
+  const int se = E - 948;  // FP32 biased exponent of 2^(E-1075)
+  const float scale = (se >= 1 && se <= 254) ? __uint_as_float((unsigned)se << 23) : 0.f;
+  const float l = __fmul_rn(__int2float_rn(n), scale);
+  return {__uint_as_float(sign | f), __uint_as_float(__float_as_uint(l) ^ sign)};
 }
 // x + d in FP64 (two FP64 additions; x keeps all of its bits)
 __device__ __forceinline__ double add_df(double x, df d) { return (x + f2d(d.hi)) + f2d(d.lo); }
@@ -275,6 +327,32 @@ __global__ void setup_faces(const fvh_mesh_view m, workspace w) {
   }
 }
 
+// ELL vertex-offset table, computed exactly as the limiter's fallback computes
+// the offsets from the hi/lo coordinate splits.
+template <int D>
+__global__ void setup_lists(const fvh_mesh_view m, workspace w) {
+  using L = layout<D>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.num_cells) return;
+  float xh[3], xl[3];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    const float2 t = split(m.cell_centroid[i][c]);
+    xh[i] = t.x;
+    xl[i] = t.y;
+  }
+  const int q0 = m.cell_vertex_offsets[c], n = m.cell_vertex_offsets[c + 1] - q0;
+  for (int k = 0; k < n && k < L::W_CV; ++k) {
+    const int v = m.cell_vertices[q0 + k];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      const float2 t = split(m.vertex_coord[i][v]);
+      w.ell_vdx[((size_t)k * D + i) * w.nc + c] =
+          __fadd_rn(__fsub_rn(t.x, xh[i]), __fsub_rn(t.y, xl[i]));
+    }
+  }
+}
+
 template <int D>
 __device__ __forceinline__ void face_geo(const workspace &w, int f, float *n, float &area) {
   const float4 g = w.fgeo[f];
@@ -321,9 +399,9 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
     store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
                   d2f(s.internal_energy[c]), a);
     const float iv = w.inv_vol32[c];
-    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
-    for (int q = q0; q < q1; ++q) {
-      int f = m.cell_faces[q];
+    const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
+    for (int k = 0; k < nq; ++k) {
+      int f = m.cell_faces[q0 + k];
       f = f < 0 ? ~f : f;
       float n[D], area;
       face_geo<D>(w, f, n, area);
@@ -376,8 +454,9 @@ pack_dt_batch_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
                   d2f(s.internal_energy[c]), a);
     const float iv = w.inv_vol32[c];
-    for (int q = m.cell_face_offsets[c]; q < m.cell_face_offsets[c + 1]; ++q) {
-      int f = m.cell_faces[q];
+    const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
+    for (int k = 0; k < nq; ++k) {
+      int f = m.cell_faces[q0 + k];
       f = f < 0 ? ~f : f;
       float n[D], area;
       face_geo<D>(w, f, n, area);
@@ -436,25 +515,26 @@ __global__ void dt_final_batch_kernel(const problem_map pm, fvh_device_status du
 // ---------------------------------------------------------------------------
 // FP32 gradients + Barth-Jespersen vertex limiter
 // ---------------------------------------------------------------------------
-template <int D, bool LIMIT, int BS>
-__global__ void __launch_bounds__(BS, 1024 / BS)
-gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk) {
+// Gradient and limiter arithmetic of one cell c0, shared by the kernels below;
+// nbr(k, u1, yh, yl) supplies neighbour k's pack values and centroid.
+template <int D>
+__device__ __forceinline__ void pack_values(const prim<float, D> &p, float *u) {
+  int k = 0;
+  u[k++] = p.d;
+#pragma unroll
+  for (int d = 0; d < D; ++d) u[k++] = p.v[d];
+  u[k++] = p.e;
+  u[k++] = p.p;
+  u[k++] = p.a;
+}
+
+template <int D, bool LIMIT, int UNROLL, class NBR>
+__device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const workspace &w,
+                                               int c0, const float *u0, const float *xh,
+                                               const float *xl, int nn, NBR nbr) {
   constexpr int NV = D + 4;
   constexpr float tol = 1.e-9f;
-  for (int c0 = blockIdx.x * BS + threadIdx.x; c0 < m.num_cells; c0 += gridDim.x * BS) {
-  float xh[3], xl[3];
-  load_cen<D>(w.ccen, c0, xh, xl);
-  float u0[NV], umin[NV], umax[NV];
-  {
-    const prim<float, D> p = load_pack<D>(pk, c0);
-    int k = 0;
-    u0[k++] = p.d;
-#pragma unroll
-    for (int d = 0; d < D; ++d) u0[k++] = p.v[d];
-    u0[k++] = p.e;
-    u0[k++] = p.p;
-    u0[k++] = p.a;
-  }
+  float umin[NV], umax[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
   float M[6] = {0, 0, 0, 0, 0, 0};
@@ -463,23 +543,10 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
   for (int k = 0; k < NV; ++k)
 #pragma unroll
     for (int j = 0; j < D; ++j) b[k][j] = 0.f;
-  const int q0 = m.cell_nbr_offsets[c0], q1 = m.cell_nbr_offsets[c0 + 1];
-#pragma unroll 4
-  for (int q = q0; q < q1; ++q) {
-    const int c1 = m.cell_nbrs[q];
-    const prim<float, D> p = load_pack<D>(pk, c1);
-    float u1[NV];
-    {
-      int k = 0;
-      u1[k++] = p.d;
-#pragma unroll
-      for (int d = 0; d < D; ++d) u1[k++] = p.v[d];
-      u1[k++] = p.e;
-      u1[k++] = p.p;
-      u1[k++] = p.a;
-    }
-    float yh[3], yl[3], dx[3];
-    load_cen<D>(w.ccen, c1, yh, yl);
+#pragma unroll UNROLL
+  for (int q = 0; q < nn; ++q) {
+    float u1[NV], yh[3], yl[3], dx[3];
+    nbr(q, u1, yh, yl);
 #pragma unroll
     for (int i = 0; i < D; ++i) dx[i] = (yh[i] - xh[i]) + (yl[i] - xl[i]);
     if (D == 2) {
@@ -533,13 +600,8 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
     float dpos[NV], dneg[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) dpos[k] = dneg[k] = 0.f;
-    const int r0 = m.cell_vertex_offsets[c0], r1 = m.cell_vertex_offsets[c0 + 1];
-    for (int r = r0; r < r1; ++r) {
-      const int vtx = m.cell_vertices[r];
-      float vh[3], vl[3], dxv[3];
-      load_cen<D>(w.vcoord, vtx, vh, vl);
-#pragma unroll
-      for (int i = 0; i < D; ++i) dxv[i] = (vh[i] - xh[i]) + (vl[i] - xl[i]);
+    const int r0 = m.cell_vertex_offsets[c0], nr = m.cell_vertex_offsets[c0 + 1] - r0;
+    auto vertex = [&](const float *dxv) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
         float du = 0.f;
@@ -548,6 +610,21 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
         dpos[k] = fmaxf(du, dpos[k]);
         dneg[k] = fminf(du, dneg[k]);
       }
+    };
+    const int ne = nr < layout<D>::W_CV ? nr : layout<D>::W_CV;
+    const float *vd = w.ell_vdx + c0;
+    for (int r = 0; r < ne; ++r, vd += (size_t)D * w.nc) {  // ELL offsets
+      float dxv[3];
+#pragma unroll
+      for (int i = 0; i < D; ++i) dxv[i] = vd[(size_t)i * w.nc];
+      vertex(dxv);
+    }
+    for (int r = ne; r < nr; ++r) {  // beyond the ELL width: from the coordinates
+      float vh[3], vl[3], dxv[3];
+      load_cen<D>(w.vcoord, m.cell_vertices[r0 + r], vh, vl);
+#pragma unroll
+      for (int i = 0; i < D; ++i) dxv[i] = __fadd_rn(__fsub_rn(vh[i], xh[i]), __fsub_rn(vl[i], xl[i]));
+      vertex(dxv);
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -571,7 +648,26 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
   for (int q = 0; q < G4; ++q)
     w.grads[(size_t)G4 * c0 + q] =
         make_float4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
-  }  // cells
+}
+
+// Neighbour records are loaded as the loop reaches them.  3D keeps
+// 7 x 3 gradient sums, 14 extrema and the 3x3 system live: up to 128
+// registers there, 64 in 2D.
+template <int D, bool LIMIT, int BS>
+__global__ void __launch_bounds__(BS, (D == 2 ? 1024 : 512) / BS)
+gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk) {
+  for (int c0 = blockIdx.x * BS + threadIdx.x; c0 < m.num_cells; c0 += gridDim.x * BS) {
+    float xh[3], xl[3], u0[D + 4];
+    load_cen<D>(w.ccen, c0, xh, xl);
+    pack_values<D>(load_pack<D>(pk, c0), u0);
+    const int q0 = m.cell_nbr_offsets[c0], nn = m.cell_nbr_offsets[c0 + 1] - q0;
+    cell_gradients<D, LIMIT, 4>(m, w, c0, u0, xh, xl, nn,
+                                [&](int q, float *u1, float *yh, float *yl) {
+                                  const int c1 = m.cell_nbrs[q0 + q];
+                                  pack_values<D>(load_pack<D>(pk, c1), u1);
+                                  load_cen<D>(w.ccen, c1, yh, yl);
+                                });
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -658,72 +754,123 @@ __device__ __forceinline__ bool negative(double x) {
 }
 
 // Conservative update of cell c from its compensated face sums
-// (update_state_from_flux + update_state_from_energy, tasks.h:589-659).  The
-// cell's FP64 state enters and leaves in FP64; the increments are carried in
-// double-float:
+// (update_state_from_flux + update_state_from_energy, tasks.h:589-659), in
+// the increment form
 //   rho' = rho + dU0,   v' = v + (dUm - v dU0) / rho',
 //   e'   = e + (dUE - (e + |v|^2/2) dU0) / rho' - v.dv - |dv|^2/2
-// with dU = (face sum) dt / V.  Each new FP64 value is its old value plus one
-// double-float increment, so rho'(e' + |v'|^2/2) is the old total energy plus
-// dUE to about 2^-48 relative, and the FP64 pipe does D + 2 splits and
-// 2D + 5 additions per cell.  Writes the FP64 state and the next pack record.
-template <int D>
+// with dU = (face sum) dt / V and all increments in double-float, so
+// rho'(e' + |v'|^2/2) is the old total energy plus dUE to about 2^-48 relative.
+//
+// STAGE 0 (predictor) writes no FP64 state: it keeps its increments (d rho,
+// d v.., d e) in w.delta and writes the FP32 pack of the predicted state.
+// STAGE 1 (corrector) rebuilds the predicted state from the FP64 state and
+// those increments, adds its own, and writes the FP64 state as
+//   x_new = x + (d_predictor + d_corrector)
+// so every FP64 value takes one double-float increment per time step and
+// keeps all of its bits.  FP64 pipe per step: 2(D+2) splits and 2D+5 adds.
+template <int D, int STAGE>
 __device__ __forceinline__ void cell_update(const fvh_state_view &s, const workspace &w,
                                             float4 *__restrict__ pk_out, const problem_map &pm,
                                             int c, int pr, df dts, const float *shi,
                                             const float *slo, const update_consts &k) {
+  constexpr int L4 = layout<D>::DEL4;
   const df scale = df_mul(dts, {w.inv_vol32[c], w.inv_vol_lo[c]});
   df du[D + 2];
 #pragma unroll
   for (int q = 0; q < D + 2; ++q) du[q] = df_mul({shi[q], slo[q]}, scale);
   const double den0 = s.density[c], e0 = s.internal_energy[c];
   double vel[D];
-  df v0[D];
+  df rho = df_from(den0), e = df_from(e0), v[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     vel[i] = s.velocity[i][c];
-    v0[i] = df_from(vel[i]);
+    v[i] = df_from(vel[i]);
   }
-  const df rho = df_add(df_from(den0), du[0]);
-  const float r = __frcp_rn(rho.hi);
+  float pv[4 * L4];  // predictor increments: (d rho, d v.., d e) as (hi, lo) pairs
+  if (STAGE == 1) {
+    const float4 *dp = w.delta + (size_t)L4 * c;
+    float4 t[L4];
+    if (L4 == 2) {
+      ldg256(dp, t[0], t[1]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < L4; ++q) t[q] = dp[q];
+    }
+#pragma unroll
+    for (int q = 0; q < L4; ++q) {
+      pv[4 * q] = t[q].x;
+      pv[4 * q + 1] = t[q].y;
+      pv[4 * q + 2] = t[q].z;
+      pv[4 * q + 3] = t[q].w;
+    }
+    rho = df_add(rho, {pv[0], pv[1]});
+#pragma unroll
+    for (int i = 0; i < D; ++i) v[i] = df_add(v[i], {pv[2 + 2 * i], pv[3 + 2 * i]});
+    e = df_add(e, {pv[2 * D + 2], pv[2 * D + 3]});
+  }
+  const df rho2 = df_add(rho, du[0]);
+  const float r = __frcp_rn(rho2.hi);
   df k0 = {0.f, 0.f}, dv[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    k0 = df_add(k0, df_mul(v0[i], v0[i]));
-    dv[i] = df_div(df_sub(du[1 + i], df_mul(v0[i], du[0])), rho, r);
+    k0 = df_add(k0, df_mul(v[i], v[i]));
+    dv[i] = df_div(df_sub(du[1 + i], df_mul(v[i], du[0])), rho2, r);
   }
-  const df e0d = df_from(e0);
-  df de = df_div(df_sub(du[D + 1], df_mul(df_add(e0d, df_half(k0)), du[0])), rho, r);
+  df de = df_div(df_sub(du[D + 1], df_mul(df_add(e, df_half(k0)), du[0])), rho2, r);
   df vdv = {0.f, 0.f}, dv2 = {0.f, 0.f};
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    vdv = df_add(vdv, df_mul(v0[i], dv[i]));
+    vdv = df_add(vdv, df_mul(v[i], dv[i]));
     dv2 = df_add(dv2, df_mul(dv[i], dv[i]));
   }
   de = df_sub(de, df_add(vdv, df_half(dv2)));
-  const double mass = add_df(den0, du[0]);
+  const df e2 = df_add(e, de);
+  const df pd = df_mul(k.gm1, df_mul(rho2, e2));
+  const float a = sqrtf(k.ggm1 * e2.hi);
+  if (STAGE == 0) {
+    float t[4 * L4];
+    t[0] = du[0].hi;
+    t[1] = du[0].lo;
 #pragma unroll
-  for (int i = 0; i < D; ++i) vel[i] = add_df(vel[i], dv[i]);
-  const double e = add_df(e0, de);
-  const df pd = df_mul(k.gm1, df_mul(rho, df_add(e0d, de)));
-  const double p = f2d(pd.hi) + f2d(pd.lo);
-  const float ef = d2f(e);
-  const float a = sqrtf(k.ggm1 * ef);
-  s.density[c] = mass;
+    for (int i = 0; i < D; ++i) {
+      t[2 + 2 * i] = dv[i].hi;
+      t[3 + 2 * i] = dv[i].lo;
+    }
+    t[2 * D + 2] = de.hi;
+    t[2 * D + 3] = de.lo;
 #pragma unroll
-  for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
-  s.internal_energy[c] = e;
-  s.pressure[c] = p;
-  s.temperature[c] = k.unit_cv ? e : e * k.inv_cv;
-  s.sound_speed[c] = f2d(a);
-  if (pk_out) {
+    for (int q = 2 * D + 4; q < 4 * L4; ++q) t[q] = 0.f;
+    float4 *dp = w.delta + (size_t)L4 * c;
+    if (L4 == 2) {
+      stg256(dp, make_float4(t[0], t[1], t[2], t[3]), make_float4(t[4], t[5], t[6], t[7]));
+    } else {
+#pragma unroll
+      for (int q = 0; q < L4; ++q)
+        dp[q] = make_float4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
+    }
     float vf[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i) vf[i] = d2f(vel[i]);
-    store_pack<D>(pk_out, c, d2f(mass), vf, d2f(p), ef, a);
+    for (int i = 0; i < D; ++i) vf[i] = df_add(v[i], dv[i]).hi;
+    store_pack<D>(pk_out, c, rho2.hi, vf, pd.hi, e2.hi, a);
+    if (e2.hi < 0.f || rho2.hi < 0.f)
+      atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
+  } else {
+    const double mass = add_df(den0, df_add({pv[0], pv[1]}, du[0]));
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+      vel[i] = add_df(vel[i], df_add({pv[2 + 2 * i], pv[3 + 2 * i]}, dv[i]));
+    const double en = add_df(e0, df_add({pv[2 * D + 2], pv[2 * D + 3]}, de));
+    const double p = f2d(pd.hi) + f2d(pd.lo);
+    s.density[c] = mass;
+#pragma unroll
+    for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
+    s.internal_energy[c] = en;
+    s.pressure[c] = p;
+    s.temperature[c] = k.unit_cv ? en : en * k.inv_cv;
+    s.sound_speed[c] = f2d(a);
+    if (negative(en) || negative(mass))
+      atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
   }
-  if (negative(e) || negative(mass))
-    atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
 }
 
 // Per-thread cache of the stage's dt for the problem of the current cell; the
@@ -749,32 +896,32 @@ struct stage_dt {
 };
 
 // Cell-centric schedule: each cell evaluates the fluxes of its own faces.
-template <int D, int KIND, bool SECOND, int BS>
+template <int D, int KIND, bool SECOND, int BS, int STAGE>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                    const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out,
-                   const problem_map pm, const update_consts k, int swap, int outflow) {
-  // Reads only pk_in (all cells) and the cell's own FP64 state; writes the
-  // cell's FP64 state and its pk_out record (null after the corrector).
+                   const problem_map pm, const update_consts uc, int swap, int outflow) {
+  // Reads pk_in (all cells) and the cell's own FP64 state; the predictor writes
+  // the cell's increments and pk_out record, the corrector its FP64 state.
   stage_dt sdt;
   for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    if (!sdt.at(pm, c, pr, k.factor)) continue;
+    if (!sdt.at(pm, c, pr, uc.factor)) continue;
     // face sums in FP32 with error-free two-sum compensation (hi + lo carries
     // about 48 bits)
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
-    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
+    const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
 #pragma unroll 2
-    for (int q = q0; q < q1; ++q) {
-      const int sf = m.cell_faces[q];
+    for (int k = 0; k < nq; ++k) {
+      const int sf = m.cell_faces[q0 + k];
       float F[D + 2];
       face_flux_area<D, KIND, SECOND>(m, w, pk_in, sf < 0 ? ~sf : sf, swap, outflow, F);
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, k);
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc);
   }
 }
 
@@ -796,22 +943,22 @@ face_flux_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 }
 
 // Face schedule, part 2: cell-centric gather of the face-flux array + update.
-template <int D, int BS>
+template <int D, int BS, int STAGE>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                      float4 *__restrict__ pk_out, const problem_map pm,
-                     const update_consts k) {
+                     const update_consts uc) {
   constexpr int F4 = layout<D>::FLUX4;
   stage_dt sdt;
   for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    if (!sdt.at(pm, c, pr, k.factor)) continue;
+    if (!sdt.at(pm, c, pr, uc.factor)) continue;
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
-    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
-    for (int q = q0; q < q1; ++q) {
-      const int sf = m.cell_faces[q];
+    const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
+    for (int k = 0; k < nq; ++k) {
+      const int sf = m.cell_faces[q0 + k];
       const int f = sf < 0 ? ~sf : sf;
       float F[4 * F4];
 #pragma unroll
@@ -825,8 +972,30 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, k);
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc);
   }
+}
+
+// Diagnostic: the integer-pipe conversions applied to an array, so they can be
+// compared with exact host conversions.
+__global__ void split_kernel(const double *x, int64_t n, float *hi, float *lo, float *h2,
+                             double *back) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const df d = df_from(x[i]);
+    hi[i] = d.hi;
+    lo[i] = d.lo;
+    h2[i] = d2f(x[i]);
+    back[i] = f2d(d.hi);
+  }
+}
+
+cudaError_t debug_split(const double *x, int64_t n, float *hi, float *lo, float *h2,
+                        double *back, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t nb = (n + 255) / 256;
+  split_kernel<<<(int)(nb < 4096 ? nb : 4096), 256, 0, st>>>(x, n, hi, lo, h2, back);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -836,8 +1005,10 @@ template <int D>
 static size_t bytes_for(int nc, int nf, int nv) {
   using L = layout<D>;
   return sizeof(float4) * ((size_t)nc * (2 * L::PACK4 + L::GRAD4 + L::CEN4) + (size_t)nv * L::CEN4 +
-                           (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4)) +
-         2 * sizeof(float) * (size_t)nc + 256 * 9;
+                           (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4) + (size_t)nc * L::DEL4) +
+         2 * sizeof(float) * (size_t)nc +
+         sizeof(float) * (size_t)nc * L::W_CV * D +
+         256 * 12;
 }
 
 template <int D>
@@ -857,8 +1028,10 @@ static void carve(workspace *w) {
   w->fgeo = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FGEO4));
   w->fdx = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FDX4));
   w->fflux = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nf * L::FLUX4));
+  w->delta = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nc * L::DEL4));
   w->inv_vol32 = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
   w->inv_vol_lo = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
+  w->ell_vdx = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc * L::W_CV * D));
 }
 
 template <int D>
@@ -867,6 +1040,7 @@ static cudaError_t setup_d(const fvh_mesh_view &m, workspace *w, cudaStream_t st
   setup_cells<D><<<(m.num_cells + t - 1) / t, t, 0, st>>>(m, *w);
   setup_vertices<D><<<(m.num_vertices + t - 1) / t, t, 0, st>>>(m, *w);
   setup_faces<D><<<(m.num_faces + t - 1) / t, t, 0, st>>>(m, *w);
+  setup_lists<D><<<(m.num_cells + t - 1) / t, t, 0, st>>>(m, *w);
   return cudaGetLastError();
 }
 
@@ -951,11 +1125,18 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
     face_flux_kernel<D, KIND, SECOND, BS><<<nbf, BS, 0, st>>>(m, *w, pk_in, p.recon_swap_ep,
                                                                p.boundary);
     mark("face_flux");
-    gather_update_kernel<D, BS><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
+    if (stage == 0)
+      gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
+    else
+      gather_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
     mark("gather_update");
   } else {
-    flux_update_kernel<D, KIND, SECOND, BS><<<nb, BS, 0, st>>>(
-        m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
+    if (stage == 0)
+      flux_update_kernel<D, KIND, SECOND, BS, 0><<<nb, BS, 0, st>>>(
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
+    else
+      flux_update_kernel<D, KIND, SECOND, BS, 1><<<nb, BS, 0, st>>>(
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
     mark("flux_update");
   }
 }

@@ -75,5 +75,10 @@ cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p
                        const launch_shape &shape, cudaStream_t st,
                        const launch_mark &mark = launch_mark());
 
+// Diagnostic: hi/lo of the integer-pipe FP64 -> double-float split, the FP64
+// -> FP32 conversion and the FP32 -> FP64 conversion of hi, for x[0..n).
+cudaError_t debug_split(const double *x, int64_t n, float *hi, float *lo, float *h2,
+                        double *back, cudaStream_t st);
+
 }  // namespace mixed
 }  // namespace fvh

@@ -136,6 +136,7 @@ def _declare(L: C.CDLL) -> None:
                                               C.POINTER(C.c_double), vp]),
         "fvh_solver_launches_per_step": (C.c_int32, [vp]),
         "fvh_solver_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
+        "fvh_debug_split": (C.c_int, [vp, C.c_int64, vp, vp, vp, vp, vp]),
         "fvh_solver_autotune": (C.c_int, [vp, C.POINTER(StateView), C.c_int32,
                                           C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32), C.POINTER(C.c_double), vp]),

@@ -285,6 +285,13 @@ int32_t fvh_solver_launches_per_step(const fvh_solver *s);
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule);
 
+/* Diagnostic of the mixed form's integer-pipe conversions on device arrays of
+ * n elements: hi/lo = the double-float split of x (hi + lo = x to about 2^-48),
+ * rn32 = x rounded to FP32 (FP32 subnormals flush to zero), hi_as_double = hi
+ * converted back to FP64.  No reference counterpart. */
+fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, float *rn32,
+                           double *hi_as_double, fvh_stream_t stream);
+
 /* Times each candidate launch shape for trial_steps steps on a scratch copy
  * of `state` and keeps the fastest; the state, solution time and status word
  * are left unchanged.  Synchronises; allocates the scratch copy.  No

@@ -128,3 +128,55 @@ def test_solver_shapes_bitwise_equal(cuda, dim):
     assert np.array_equal(dstate.download(), outs[0][0])
     with pytest.raises(H.FvhError):
         solver.set_shape(64, 1, 0)
+
+
+def _split_cases():
+    rng = np.random.default_rng(11)
+    f = (rng.uniform(1, 2, 4000) * 2.0 ** rng.integers(-70, 120, 4000)).astype(np.float32)
+    f = f * np.where(rng.random(4000) < 0.5, -1, 1).astype(np.float32)
+    ulp = np.spacing(np.abs(f)).astype(np.float64)
+    fd = f.astype(np.float64)
+    ties = fd + 0.5 * ulp                       # exact halfway cases: round to even
+    near = fd + 0.5 * ulp * (1 - 2.0 ** -20)    # just below halfway
+    carry = 2.0 ** rng.integers(-70, 120, 500) * (1 - 2.0 ** -25)  # rounds up a binade
+    rand = rng.standard_normal(20000) * 10.0 ** rng.uniform(-20, 30, 20000)
+    special = np.array([0.0, -0.0, 1e-300, -1e-300, 2.0 ** -127, 2.0 ** -100, 1e39, -1e39,
+                        np.inf, -np.inf, 1.0, -1.0, 0.1, 1.0 / 3.0])
+    return np.concatenate([ties, near, carry, rand, special, fd])
+
+
+def test_integer_pipe_conversions_exact(cuda):
+    """The mixed form's FP64 -> FP32 rounding and FP64 -> double-float split
+    run on the integer pipe; they must equal IEEE round-to-nearest-even
+    exactly: hi = RN32(x), lo = RN32(x - hi) for |x| >= 2^-74 (lo = 0 below),
+    FP32 subnormals flush to zero, hi converts back to FP64 exactly."""
+    torch = cuda
+    x = _split_cases()
+    n = x.size
+    xd = torch.from_numpy(x).cuda()
+    hi, lo, rn = (torch.empty(n, dtype=torch.float32, device="cuda") for _ in range(3))
+    back = torch.empty(n, dtype=torch.float64, device="cuda")
+    H.check(H.lib().fvh_debug_split(xd.data_ptr(), n, hi.data_ptr(), lo.data_ptr(),
+                                    rn.data_ptr(), back.data_ptr(), None), "fvh_debug_split")
+    torch.cuda.synchronize()
+    hi, lo, rn, back = (t.cpu().numpy() for t in (hi, lo, rn, back))
+    with np.errstate(over="ignore", invalid="ignore"):
+        ref = x.astype(np.float32)
+        ref_lo = (x - ref.astype(np.float64)).astype(np.float32)
+    ax = np.abs(x)
+    ref = np.where(ax < 2.0 ** -126, np.copysign(np.float32(0), x), ref).astype(np.float32)
+    ref_lo = np.where((ax < 2.0 ** -74) | ~np.isfinite(ref), np.float32(0), ref_lo)
+    assert np.array_equal(rn.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(hi.view(np.uint32), ref.view(np.uint32))
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.abs(lo[fin]), np.abs(ref_lo[fin]))
+    assert np.array_equal(lo[fin] == 0, ref_lo[fin] == 0)
+    assert np.array_equal(np.sign(lo[fin]), np.sign(ref_lo[fin]))
+    assert np.array_equal(back[fin], ref[fin].astype(np.float64))
+    nan = np.array([np.nan])
+    xd = torch.from_numpy(nan).cuda()
+    h1, l1, r1 = (torch.empty(1, dtype=torch.float32, device="cuda") for _ in range(3))
+    b1 = torch.empty(1, dtype=torch.float64, device="cuda")
+    H.check(H.lib().fvh_debug_split(xd.data_ptr(), 1, h1.data_ptr(), l1.data_ptr(),
+                                    r1.data_ptr(), b1.data_ptr(), None), "fvh_debug_split")
+    assert np.isnan(r1.cpu().numpy()[0]) and np.isnan(h1.cpu().numpy()[0])
