@@ -738,7 +738,7 @@ fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cac
 int32_t fvh_batch_num_problems(const fvh_batch *b) { return b ? b->nproblems : 0; }
 int64_t fvh_batch_num_cells(const fvh_batch *b) { return b ? b->view.num_cells : 0; }
 int32_t fvh_batch_launches_per_step(const fvh_batch *b) {
-  return b ? fvh::mixed::launches_per_step(b->params, b->shape) : 0;
+  return b ? fvh::mixed::launches_per_step_batch(b->params, b->shape) : 0;
 }
 
 }  // extern "C"

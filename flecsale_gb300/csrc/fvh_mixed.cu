@@ -1,25 +1,30 @@
 // Mixed-precision form of the hydro step (sm_103a).
 //
-// Reconstruction, limiter and Riemann fluxes run in FP32; the cell state, the
-// face-to-cell accumulation, the conservative update and the dt reduction stay
-// in FP64.  Per time step (the structure of apps/hydro/driver.h:325-375):
+// Reconstruction, limiter and Riemann fluxes run in FP32; the cell state stays
+// in FP64 and takes its increments in double-float (FP32 pairs, ~48 bits) from
+// compensated FP32 face sums; dt is reduced in FP32 and finished in FP64.
+// GB300 executes FP64 at 2 operations per clock per SM (FP32: 128), so the
+// FP64 pipe is kept to the splits and final additions of the state.  Per time
+// step (the structure of apps/hydro/driver.h:325-375):
 //
-//   pack_dt      FP64 state -> FP32 recon pack (AoS, 32 B/cell) and the
-//                per-block max of (a+|v.n|) A/V for the CFL step (tasks.h:331-376)
-//   dt_final     one block: dt = min(CFL/max, t_f - t) in FP64
+//   pack_dt      FP64 state -> FP32 recon pack (AoS, 32 B/cell); CFL maximum of
+//                (a+|v.n|) A/V per block, the last block finishes dt
+//                (tasks.h:331-376)
 //   gradients    FP32 vertex-neighbour least squares + Barth-Jespersen limiter
 //                (tasks.h:145-321), FP32 AoS gradients
-//   flux_update  cell-centric: for each face of the cell, reconstruct both
-//                sides at the face centroid, Riemann/wall flux in FP32
-//                (tasks.h:385-464), accumulate -/+F in FP64 in the cell's face
-//                order, then the conservative FP64 update + EOS closure
-//                (tasks.h:589-659); writes the FP64 state and, after the
-//                predictor, the next FP32 pack
-//   (gradients, flux_update again for the corrector)
+//   schedule 0:  flux_update: each cell reconstructs both sides of each of its
+//                faces, evaluates the Riemann/wall flux in FP32
+//                (tasks.h:385-464) and sums -/+F in its face order, then
+//                updates (tasks.h:589-659)
+//   schedule 1:  face_flux (one flux per face into an array) + gather_update
+//                (the same sums in the same order, then the update)
+//   predictor update: writes the double-float increments and the FP32 pack of
+//                the predicted state, no FP64 state
+//   (gradients, fluxes again for the corrector, whose update writes the FP64
+//   state = old state + both stages' increments)
 //
-// A face shared by two cells is evaluated by both with identical inputs and
-// identical instructions, so both cells see the same bits: the update is
-// conservative to FP64 rounding without a flux array in HBM and without atomics.
+// A face flux has the same bits wherever it is evaluated, so the update is
+// conservative to double-float rounding without atomics.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -70,6 +75,7 @@ struct workspace {
   // first W_CV vertices, [(k * D + i) * nc + c]: a warp's 32 consecutive cells
   // read 32 consecutive words, with no dependent index load
   float *ell_vdx = nullptr;
+  unsigned *ticket = nullptr;  // blocks of pack_dt done (the last one computes dt)
 };
 
 __device__ __forceinline__ void stg256(float4 *p, float4 a, float4 b) {
@@ -385,9 +391,13 @@ __device__ __forceinline__ float block_max_f(float v) {
 // ---------------------------------------------------------------------------
 // pack + dt partial maxima
 // ---------------------------------------------------------------------------
+// Also computes dt: every block publishes its maximum and the last block to
+// finish (a ticket counter, reset by that block) reduces them in FP64.
 template <int D>
 __global__ void __launch_bounds__(kDtThreads)
-pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, double *partial) {
+pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, double *partial,
+               const fvh_params p, const double *soln_time, double *dt_out,
+               fvh_device_status *status) {
   // writes w.pack, the input of the predictor
   float dt_inv = 0.f;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.num_cells;
@@ -410,27 +420,33 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
     }
   }
   dt_inv = block_max_f(dt_inv);
-  if (threadIdx.x == 0) partial[blockIdx.x] = f2d(dt_inv);
-}
-
-__global__ void __launch_bounds__(kDtThreads)
-dt_final_kernel(const double *partial, int nblocks, fvh_params p, const double *soln_time,
-                double *dt_out, fvh_device_status *status) {
-  double dt_inv = 0;
-  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) dt_inv = smax(partial[i], dt_inv);
-  dt_inv = block_max(dt_inv);
+  __shared__ bool last;
   if (threadIdx.x == 0) {
+    partial[blockIdx.x] = f2d(dt_inv);
+    __threadfence();
+    last = atomicAdd(w.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+    v = smax(reinterpret_cast<volatile const double *>(partial)[i], v);
+  v = block_max(v);
+  if (threadIdx.x == 0) {
+    *w.ticket = 0u;
     const double max_dt = p.final_time - soln_time[0];
-    if (dt_inv <= 0) {
+    if (v <= 0) {
       atomicMin(status, status_key(0, FVH_ERR_INFINITE_DT));
       dt_out[0] = 0;
     } else {
-      double time_step = 1 / dt_inv;
+      double time_step = 1 / v;
       time_step *= p.cfl;
       dt_out[0] = smin(time_step, max_dt);
     }
   }
 }
+
 
 // Batch form: per-problem maxima.  A block (or warp) whose cells all belong to
 // one problem reduces first and issues one integer atomicMax on the FP32 bits
@@ -767,7 +783,8 @@ __device__ __forceinline__ bool negative(double x) {
 // those increments, adds its own, and writes the FP64 state as
 //   x_new = x + (d_predictor + d_corrector)
 // so every FP64 value takes one double-float increment per time step and
-// keeps all of its bits.  FP64 pipe per step: 2(D+2) splits and 2D+5 adds.
+// keeps all of its bits.  FP64 pipe per step: 2D+5 additions (the splits run
+// on the integer pipe).
 template <int D, int STAGE>
 __device__ __forceinline__ void cell_update(const fvh_state_view &s, const workspace &w,
                                             float4 *__restrict__ pk_out, const problem_map &pm,
@@ -1008,7 +1025,7 @@ static size_t bytes_for(int nc, int nf, int nv) {
                            (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4) + (size_t)nc * L::DEL4) +
          2 * sizeof(float) * (size_t)nc +
          sizeof(float) * (size_t)nc * L::W_CV * D +
-         256 * 12;
+         256 * 16;  // alignment of each carved array + the ticket
 }
 
 template <int D>
@@ -1032,6 +1049,7 @@ static void carve(workspace *w) {
   w->inv_vol32 = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
   w->inv_vol_lo = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
   w->ell_vdx = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc * L::W_CV * D));
+  w->ticket = reinterpret_cast<unsigned *>(take(256));
 }
 
 template <int D>
@@ -1182,10 +1200,8 @@ static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params
                           const fvh_state_view &s, double *t, double *dt, double *partial,
                           int dt_blocks, fvh_device_status *status, cudaStream_t st,
                           const launch_mark &mark, const launch_shape &shape) {
-  pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial);
+  pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial, p, t, dt, status);
   mark("pack_dt");
-  dt_final_kernel<<<1, kDtThreads, 0, st>>>(partial, dt_blocks, p, t, dt, status);
-  mark("dt_final");
   problem_map pm;
   pm.dt = dt;
   pm.t = t;
@@ -1226,7 +1242,11 @@ cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p
 
 int launches_per_step(const fvh_params &p, const launch_shape &sh) {
   const int per_stage = (p.order == 1 ? 0 : 1) + (sh.schedule == 1 ? 2 : 1);
-  return 2 + 2 * per_stage;
+  return 1 + 2 * per_stage;
+}
+
+int launches_per_step_batch(const fvh_params &p, const launch_shape &sh) {
+  return launches_per_step(p, sh) + 1;  // per-problem dt is a separate kernel
 }
 
 int launches_per_step(const fvh_params &p) { return launches_per_step(p, launch_shape()); }

@@ -54,6 +54,7 @@ cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
 int launches_per_step(const fvh_params &p, const launch_shape &sh);
+int launches_per_step_batch(const fvh_params &p, const launch_shape &sh);
 
 // Independent problems concatenated into one mesh: problem k owns the cells
 // [first_cell[k], first_cell[k+1]).  All arrays are device memory.
