@@ -36,7 +36,12 @@ UNITS = [
     ("fvh_capi.cu", []),
     ("fvh_noalloc.cu", []),
     ("fvh_batch.cu", []),
+    ("fvh_lua.cpp", []),
+    ("fvh_input.cpp", []),
 ]
+# the command-line driver (apps/hydro's executable), linked against the library
+DRIVER_SRC = "fvh_driver.cpp"
+DRIVER = os.path.join(PKG, "flecsale_hydro")
 
 
 def _nvcc() -> str:
@@ -85,6 +90,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", INCLUDE,
+           os.path.join(CSRC, DRIVER_SRC), "-o", DRIVER + ".tmp", "-L", PKG, "-lflecsale_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
     return LIB
 
 

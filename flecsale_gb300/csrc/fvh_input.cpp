@@ -1,0 +1,196 @@
+// Input files of apps/hydro: the Lua "hydro" table read by
+// apps/hydro/inputs.h:100-135 (prefix, postfix, output_freq, CFL, final_time,
+// max_steps, eos = {type, gas_constant, specific_heat}, ics = function), plus
+// the box mesh table of apps/hydro/3d/shock_box_3d.lua.  Evaluated with the
+// Lua-subset interpreter of fvh_lua.cpp.
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "flecsale_gb300.h"
+#include "fvh_internal.h"
+#include "fvh_lua.h"
+
+using fvh::lua::Value;
+
+struct fvh_input {
+  fvh::lua::State state;
+};
+
+namespace {
+
+void set_err(char *err, size_t len, const std::string &m) {
+  if (!err || len == 0) return;
+  const size_t n = m.size() < len - 1 ? m.size() : len - 1;
+  std::memcpy(err, m.data(), n);
+  err[n] = '\0';
+}
+
+Value at(const fvh_input *in, const std::string &path) {
+  const size_t dot = path.find_first_of(".[");
+  const std::string head = path.substr(0, dot);
+  const Value g = in->state.global(head);
+  return dot == std::string::npos ? g : fvh::lua::lookup(g, path.substr(dot));
+}
+
+bool as_number(const Value &v, double *out) {
+  if (v.kind == Value::NUMBER) {
+    *out = v.n;
+    return true;
+  }
+  if (v.kind == Value::STRING) {  // "1e6": Lua converts numeric strings
+    char *e = nullptr;
+    const double d = std::strtod(v.s.c_str(), &e);
+    if (e != v.s.c_str() && *e == '\0') {
+      *out = d;
+      return true;
+    }
+  }
+  return false;
+}
+
+fvh_status load(const std::string &text, const std::string &name, char *err, size_t err_len,
+                fvh_input **out) {
+  fvh_input *in = new (std::nothrow) fvh_input();
+  if (!in) return FVH_ERR_OUT_OF_MEMORY;
+  try {
+    in->state.run(text, name);
+  } catch (const std::exception &e) {
+    set_err(err, err_len, e.what());
+    delete in;
+    return FVH_ERR_INVALID_ARGUMENT;
+  }
+  if (in->state.global("hydro").kind != Value::TABLE) {
+    set_err(err, err_len, name + ": no table 'hydro'");
+    delete in;
+    return FVH_ERR_INVALID_ARGUMENT;
+  }
+  *out = in;
+  return FVH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fvh_status fvh_input_load(const char *path, char *err, size_t err_len, fvh_input **out) {
+  if (!path || !out) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::ifstream f(path, std::ios::binary);
+  if (!f) {
+    set_err(err, err_len, std::string("cannot open ") + path);
+    return FVH_ERR_INVALID_ARGUMENT;
+  }
+  std::stringstream ss;
+  ss << f.rdbuf();
+  // the chunk name Lua would report: the file name
+  std::string name = path;
+  const size_t slash = name.find_last_of('/');
+  if (slash != std::string::npos) name = name.substr(slash + 1);
+  return load(ss.str(), name, err, err_len, out);
+}
+
+fvh_status fvh_input_load_string(const char *text, char *err, size_t err_len, fvh_input **out) {
+  if (!text || !out) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  return load(text, "input", err, err_len, out);
+}
+
+void fvh_input_destroy(fvh_input *in) { delete in; }
+
+fvh_status fvh_input_number(const fvh_input *in, const char *path, double *value) {
+  if (!in || !path || !value) return FVH_ERR_INVALID_ARGUMENT;
+  return as_number(at(in, path), value) ? FVH_OK : FVH_ERR_INVALID_ARGUMENT;
+}
+
+fvh_status fvh_input_string(const fvh_input *in, const char *path, char *buf, size_t len) {
+  if (!in || !path || !buf || len == 0) return FVH_ERR_INVALID_ARGUMENT;
+  const Value v = at(in, path);
+  if (v.kind != Value::STRING) return FVH_ERR_INVALID_ARGUMENT;
+  if (v.s.size() + 1 > len) return FVH_ERR_CAPACITY;
+  std::memcpy(buf, v.s.c_str(), v.s.size() + 1);
+  return FVH_OK;
+}
+
+fvh_status fvh_input_params(const fvh_input *in, fvh_params *p, int64_t *max_steps,
+                            int64_t *output_freq) {
+  if (!in || !p) return FVH_ERR_INVALID_ARGUMENT;
+  double v;
+  if (as_number(at(in, "hydro.CFL"), &v)) p->cfl = v;
+  if (as_number(at(in, "hydro.final_time"), &v)) p->final_time = v;
+  if (max_steps && as_number(at(in, "hydro.max_steps"), &v)) *max_steps = (int64_t)v;
+  if (output_freq && as_number(at(in, "hydro.output_freq"), &v)) *output_freq = (int64_t)v;
+  const Value eos = at(in, "hydro.eos");
+  if (eos.kind == Value::TABLE) {
+    const Value type = fvh::lua::lookup(eos, "type");
+    if (type.kind != Value::STRING || type.s != "ideal_gas")
+      return FVH_ERR_UNSUPPORTED;  // inputs.h:129-131 "Unknown eos type"
+    if (as_number(fvh::lua::lookup(eos, "gas_constant"), &v)) p->gamma = v;
+    if (as_number(fvh::lua::lookup(eos, "specific_heat"), &v)) p->cv = v;
+  }
+  return FVH_OK;
+}
+
+fvh_status fvh_input_mesh(const fvh_input *in, fvh_host_mesh **out) {
+  if (!in || !out) return FVH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const Value mesh = at(in, "hydro.mesh");
+  if (mesh.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
+  const Value type = fvh::lua::lookup(mesh, "type");
+  if (type.kind != Value::STRING || type.s != "box") return FVH_ERR_UNSUPPORTED;
+  const Value dims = fvh::lua::lookup(mesh, "dimensions");
+  if (dims.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
+  const int dim = (int)dims.t->array.size();
+  if (dim != 2 && dim != 3) return FVH_ERR_INVALID_ARGUMENT;
+  int32_t n[3];
+  double lo[3], hi[3];
+  for (int k = 0; k < dim; ++k) {
+    double v;
+    const std::string idx = "[" + std::to_string(k + 1) + "]";
+    if (!as_number(dims.t->array[k], &v) || v < 1) return FVH_ERR_INVALID_ARGUMENT;
+    n[k] = (int32_t)v;
+    lo[k] = 0;
+    hi[k] = 1;
+    if (as_number(fvh::lua::lookup(mesh, "xmin" + idx), &v)) lo[k] = v;
+    if (as_number(fvh::lua::lookup(mesh, "xmax" + idx), &v)) hi[k] = v;
+  }
+  return fvh_host_mesh_box(dim, n, lo, hi, 0.0, 0, out);
+}
+
+fvh_status fvh_input_initial_state(const fvh_input *in, const fvh_host_mesh *m,
+                                   const fvh_params *p, double t, double *host_planes) {
+  if (!in || !m || !p || !host_planes || p->dim != m->dim) return FVH_ERR_INVALID_ARGUMENT;
+  const Value ics = at(in, "hydro.ics");
+  if (ics.kind != Value::FUNCTION) return FVH_ERR_INVALID_ARGUMENT;
+  const int D = m->dim, nc = m->nc;
+  std::vector<double> d(nc), v((size_t)D * nc), pr(nc);
+  fvh::lua::State &st = const_cast<fvh_input *>(in)->state;
+  try {
+    std::vector<Value> args(D + 1);
+    for (int c = 0; c < nc; ++c) {
+      for (int k = 0; k < D; ++k) args[k] = Value::number(m->cc[k][c]);
+      args[D] = Value::number(t);
+      const std::vector<Value> r = st.call(ics, args);
+      // initial_conditions (tasks.h:46-68): density, velocity, pressure
+      if (r.size() < 3 || r[0].kind != Value::NUMBER || r[1].kind != Value::TABLE ||
+          r[2].kind != Value::NUMBER)
+        return FVH_ERR_INVALID_ARGUMENT;
+      d[c] = r[0].n;
+      pr[c] = r[2].n;
+      for (int k = 0; k < D; ++k) {
+        const Value vk = r[1].t->get(Value::number(k + 1));
+        v[(size_t)k * nc + c] = vk.kind == Value::NUMBER ? vk.n : 0.0;
+      }
+    }
+  } catch (const std::exception &) {
+    return FVH_ERR_INVALID_ARGUMENT;
+  }
+  return fvh_host_state_from_dvp(D, nc, p->gamma, p->cv, d.data(), v.data(), pr.data(),
+                                 host_planes);
+}
+
+}  // extern "C"

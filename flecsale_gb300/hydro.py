@@ -137,6 +137,15 @@ def _declare(L: C.CDLL) -> None:
         "fvh_solver_launches_per_step": (C.c_int32, [vp]),
         "fvh_solver_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
         "fvh_debug_split": (C.c_int, [vp, C.c_int64, vp, vp, vp, vp, vp]),
+        "fvh_input_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
+        "fvh_input_load_string": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
+        "fvh_input_destroy": (None, [vp]),
+        "fvh_input_number": (C.c_int, [vp, C.c_char_p, C.POINTER(C.c_double)]),
+        "fvh_input_string": (C.c_int, [vp, C.c_char_p, C.c_char_p, C.c_size_t]),
+        "fvh_input_params": (C.c_int, [vp, C.POINTER(Params), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]),
+        "fvh_input_mesh": (C.c_int, [vp, C.POINTER(vp)]),
+        "fvh_input_initial_state": (C.c_int, [vp, vp, C.POINTER(Params), C.c_double, _dp]),
         "fvh_solver_autotune": (C.c_int, [vp, C.POINTER(StateView), C.c_int32,
                                           C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32), C.POINTER(C.c_double), vp]),
@@ -635,3 +644,58 @@ def batch_assign_device(batch: "Batch", dmeshes, cfl, final_time, keep=None, str
     check(lib().fvh_batch_assign_device(batch._h, n, arr, _dptr(cf), _dptr(tf), kp,
                                         stream_handle(stream)), "fvh_batch_assign_device")
     batch.meshes = list(dmeshes)
+
+
+class Input:
+    """An apps/hydro input file (the Lua "hydro" table, inputs.h:100-135)."""
+
+    def __init__(self, path: str | None = None, text: str | None = None):
+        self._h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        if path is not None:
+            code = lib().fvh_input_load(path.encode(), err, 512, C.byref(self._h))
+        else:
+            code = lib().fvh_input_load_string(text.encode(), err, 512, C.byref(self._h))
+        if code != 0:
+            raise FvhError(code, err.value.decode() or "fvh_input_load")
+
+    def number(self, path: str) -> float:
+        v = C.c_double()
+        check(lib().fvh_input_number(self._h, path.encode(), C.byref(v)), path)
+        return v.value
+
+    def string(self, path: str) -> str:
+        buf = C.create_string_buffer(4096)
+        check(lib().fvh_input_string(self._h, path.encode(), buf, 4096), path)
+        return buf.value.decode()
+
+    def params(self, dim: int, **kw) -> tuple:
+        """(Params, max_steps, output_freq): reference defaults for dim, then the file."""
+        p = make_params(dim, **kw)
+        ms, of = C.c_int64(-1), C.c_int64(-1)
+        check(lib().fvh_input_params(self._h, C.byref(p), C.byref(ms), C.byref(of)),
+              "fvh_input_params")
+        return p, ms.value, of.value
+
+    def mesh(self) -> "HostMesh":
+        h = C.c_void_p()
+        check(lib().fvh_input_mesh(self._h, C.byref(h)), "fvh_input_mesh")
+        return HostMesh(h)
+
+    def initial_state(self, mesh: "HostMesh", params: Params, t: float = 0.0) -> np.ndarray:
+        out = np.empty((5 + mesh.dim, mesh.num_cells), np.float64)
+        check(lib().fvh_input_initial_state(self._h, mesh._h, C.byref(params), t, _dptr(out)),
+              "fvh_input_initial_state")
+        return out
+
+    def close(self):
+        if self._h and _LIB is not None:
+            _LIB.fvh_input_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+
+def driver_path() -> str:
+    """The flecsale_hydro command-line driver built beside the library."""
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "flecsale_hydro")

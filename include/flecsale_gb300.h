@@ -435,6 +435,46 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
                                    double *host_planes, int64_t nsteps,
                                    double *soln_time, fvh_stream_t stream);
 
+
+/* ------------------------------------------------------------------------- */
+/* Input files: the Lua "hydro" table of apps/hydro/inputs.h:100-135          */
+/* ------------------------------------------------------------------------- */
+typedef struct fvh_input fvh_input;
+
+/* Parse and run a Lua input file (replaces inputs_t::load, inputs.h:83-97;
+ * the subset FleCSALE inputs use: tables, numbers, strings, and functions with
+ * locals, if/elseif/else, numeric for, while, multiple returns and the math
+ * library).  On failure *out is null and err (when given) holds
+ * "file:line: message"; the file must define a table "hydro". */
+fvh_status fvh_input_load(const char *path, char *err, size_t err_len, fvh_input **out);
+fvh_status fvh_input_load_string(const char *text, char *err, size_t err_len,
+                                 fvh_input **out);
+void fvh_input_destroy(fvh_input *in);
+
+/* Number or string at a path below the globals, e.g. "hydro.CFL",
+ * "hydro.eos.gas_constant", "hydro.mesh.dimensions[2]".  Numeric strings
+ * ("1e6", as output_freq in shock_box_2d.lua) read as numbers, as Lua converts
+ * them.  FVH_ERR_INVALID_ARGUMENT when absent or of another type. */
+fvh_status fvh_input_number(const fvh_input *in, const char *path, double *value);
+fvh_status fvh_input_string(const fvh_input *in, const char *path, char *buf, size_t len);
+
+/* The keys inputs.h:112-132 reads: CFL, final_time, eos = {type = "ideal_gas",
+ * gas_constant, specific_heat} into p (absent keys keep p's values), and
+ * max_steps and output_freq into the counters (either may be null).  Another
+ * eos type returns FVH_ERR_UNSUPPORTED (inputs.h:129-131). */
+fvh_status fvh_input_params(const fvh_input *in, fvh_params *p, int64_t *max_steps,
+                            int64_t *output_freq);
+
+/* hydro.mesh = {type = "box", dimensions = {nx, ny[, nz]}, xmin = {..}, xmax = {..}}
+ * (apps/hydro/3d/shock_box_3d.lua) as an unjittered box mesh. */
+fvh_status fvh_input_mesh(const fvh_input *in, fvh_host_mesh **out);
+
+/* Evaluate hydro.ics(x, y[, z], t) at every cell centroid; it returns density,
+ * {velocity}, pressure, closed with the ideal gas as initial_conditions does
+ * (tasks.h:46-68).  host_planes: (5+dim) x num_cells. */
+fvh_status fvh_input_initial_state(const fvh_input *in, const fvh_host_mesh *m,
+                                   const fvh_params *p, double t, double *host_planes);
+
 /* ------------------------------------------------------------------------- */
 /* Batched form: independent meshes advanced together (mixed precision)      */
 /* ------------------------------------------------------------------------- */
