@@ -97,10 +97,20 @@ struct fvh_solver {
   fvh_device_status *host_status = nullptr;
   fvh::mixed::workspace *mixed = nullptr;
   fvh::mixed::launch_shape shape;  // mixed form's cell-kernel launch shape
-  cudaGraphExec_t graph = nullptr;
+  // one CUDA graph per step variant (index: pack_first * 2 + write_next), for
+  // one (stream, state) pair
+  cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t graph_stream = nullptr;
   fvh_state_view graph_state{};
 };
+
+static void drop_graphs(fvh_solver *s) {
+  for (auto &g : s->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
 
 
 struct fvh_device_state {
@@ -233,7 +243,7 @@ fvh_status fvh_apply_update(const fvh_mesh_view *mesh, const fvh_params *params,
 // ---------------------------------------------------------------------------
 void fvh_solver_destroy(fvh_solver *s) {
   if (!s) return;
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  drop_graphs(s);
   if (s->mixed) fvh::mixed::destroy(s->mixed);
   cudaFree(s->work);
   cudaFree(s->tables);
@@ -308,13 +318,14 @@ fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params
 
 static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state,
                                       cudaStream_t st,
-                                      const fvh::mixed::launch_mark &mark = {}) {
+                                      const fvh::mixed::launch_mark &mark = {},
+                                      fvh::mixed::step_flags f = {}) {
   const fvh_mesh_view &m = s->mesh;
   const fvh_params &p = s->params;
   double *t = s->scalars, *dt = s->scalars + 1, *partial = s->scalars + 2;
   if (p.precision == FVH_PRECISION_MIXED)
     return from_cuda(fvh::mixed::step(s->mixed, m, p, *state, t, dt, partial,
-                                      dt_blocks(m.num_cells), s->status, st, mark, s->shape));
+                                      dt_blocks(m.num_cells), s->status, st, mark, s->shape, f));
   const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
   const int nb = dt_blocks(m.num_cells);
   fvh_status r = from_cuda(
@@ -337,6 +348,19 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   return r;
 }
 
+// Flags of step k of a chunk of n consecutive steps: the first recomputes the
+// pack and dt from the FP64 state, every corrector but the last writes them
+// for the following step.
+static fvh::mixed::step_flags chunk_flags(int64_t k, int64_t n) {
+  fvh::mixed::step_flags f;
+  f.pack_first = k == 0;
+  f.write_next = k + 1 < n;
+  return f;
+}
+
+static fvh_status solver_step_flags(fvh_solver *s, const fvh_state_view *state, cudaStream_t st,
+                                    fvh::mixed::step_flags f);
+
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule) {
   if (!s || (block != 128 && block != 256) || cells_per_thread < 1 || cells_per_thread > 8 ||
@@ -345,10 +369,7 @@ fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_
   s->shape.block = block;
   s->shape.cells_per_thread = cells_per_thread;
   s->shape.schedule = schedule;
-  if (s->graph) {
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
-  }
+  drop_graphs(s);
   return FVH_OK;
 }
 
@@ -414,11 +435,14 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
     if (e != cudaSuccess) break;
     fvh_solver_set_shape(s, c.block, c.cells_per_thread, c.schedule);
     refresh();
+    // timed as fvh_solver_run launches steps
     fvh_status r = FVH_OK;
-    for (int k = 0; k < trial_steps && r == FVH_OK; ++k) r = fvh_solver_step(s, &tmp, stream);
+    for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
+      r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
     refresh();
     cudaEventRecord(e0, st);
-    for (int k = 0; k < trial_steps && r == FVH_OK; ++k) r = fvh_solver_step(s, &tmp, stream);
+    for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
+      r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
     cudaEventRecord(e1, st);
     if (r == FVH_OK) e = cudaEventSynchronize(e1);
     if (r != FVH_OK || e != cudaSuccess) continue;
@@ -454,6 +478,18 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
   return from_cuda(fvh::mixed::debug_split(x, n, hi, lo, rn32, hi_as_double, cs(stream)));
 }
 
+int64_t fvh_solver_launches_per_run(const fvh_solver *s, int64_t nsteps) {
+  if (!s || nsteps <= 0) return 0;
+  if (s->params.precision != FVH_PRECISION_MIXED)
+    return nsteps * fvh_solver_launches_per_step(s);
+  int64_t total = 0;
+  for (int64_t k = 0; k < nsteps && k < 2; ++k)  // the first step and one of the rest
+    total += fvh::mixed::launches_per_step(s->params, s->shape, chunk_flags(k, nsteps));
+  if (nsteps > 2)
+    total += (nsteps - 2) * fvh::mixed::launches_per_step(s->params, s->shape, chunk_flags(1, nsteps));
+  return total;
+}
+
 int32_t fvh_solver_launches_per_step(const fvh_solver *s) {
   if (!s) return 0;
   if (s->params.precision == FVH_PRECISION_MIXED)
@@ -483,10 +519,9 @@ void profile_mark(void *vctx, const char *name) {
 
 fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_t nsteps,
                               int32_t max_kernels, const char **names, double *mean_ms,
-                              int32_t *launches_per_step, int32_t *nkernels,
-                              fvh_stream_t stream) {
+                              int32_t *launches, int32_t *nkernels, fvh_stream_t stream) {
   if (!s || !state_ok(state, s->mesh.dim) || nsteps <= 0 || max_kernels <= 0 || !names ||
-      !mean_ms || !launches_per_step || !nkernels)
+      !mean_ms || !launches || !nkernels)
     return FVH_ERR_INVALID_ARGUMENT;
   profile_ctx ctx;
   ctx.st = cs(stream);
@@ -498,7 +533,8 @@ fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_
   mark.ctx = &ctx;
   fvh_status r = FVH_OK;
   profile_mark(&ctx, "");  // start event
-  for (int k = 0; k < nsteps && r == FVH_OK; ++k) r = solver_step_enqueue(s, state, ctx.st, mark);
+  for (int k = 0; k < nsteps && r == FVH_OK; ++k)
+    r = solver_step_enqueue(s, state, ctx.st, mark, chunk_flags(k, nsteps));
   if (r == FVH_OK) r = from_cuda(cudaStreamSynchronize(ctx.st));
   int32_t nk = 0;
   if (r == FVH_OK) {
@@ -520,7 +556,7 @@ fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_
     }
     for (int k = 0; k < nk; ++k) {
       mean_ms[k] = count[k] ? total[k] / count[k] : 0.0;
-      launches_per_step[k] = count[k] / nsteps;
+      launches[k] = count[k];
     }
   }
   *nkernels = nk;
@@ -528,40 +564,42 @@ fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_
   return r;
 }
 
+// One step is a fixed sequence of launches; each variant is captured once per
+// (stream, state) into a CUDA graph and replayed.
+static fvh_status solver_step_flags(fvh_solver *s, const fvh_state_view *state, cudaStream_t st,
+                                    fvh::mixed::step_flags f) {
+  if (s->params.precision != FVH_PRECISION_MIXED) f = fvh::mixed::step_flags();
+  if (st == nullptr) return solver_step_enqueue(s, state, st, {}, f);
+  if (s->graph_stream != st || std::memcmp(&s->graph_state, state, sizeof(*state)) != 0) {
+    drop_graphs(s);
+    s->graph_stream = st;
+    s->graph_state = *state;
+  }
+  cudaGraphExec_t &ge = s->graph[(f.pack_first ? 2 : 0) + (f.write_next ? 1 : 0)];
+  if (!ge) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return from_cuda(e);
+    const fvh_status r = solver_step_enqueue(s, state, st, {}, f);
+    e = cudaStreamEndCapture(st, &g);
+    if (r != FVH_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (e != cudaSuccess) return from_cuda(e);
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      ge = nullptr;
+      return from_cuda(e);
+    }
+  }
+  return from_cuda(cudaGraphLaunch(ge, st));
+}
+
 fvh_status fvh_solver_step(fvh_solver *s, const fvh_state_view *state, fvh_stream_t stream) {
   if (!s || !state_ok(state, s->mesh.dim)) return FVH_ERR_INVALID_ARGUMENT;
-  cudaStream_t st = cs(stream);
-  // One step is a fixed sequence of launches; it is captured once per
-  // (stream, state) into a CUDA graph and replayed.
-  if (st != nullptr) {
-    if (!s->graph || s->graph_stream != st ||
-        std::memcmp(&s->graph_state, state, sizeof(*state)) != 0) {
-      if (s->graph) {
-        cudaGraphExecDestroy(s->graph);
-        s->graph = nullptr;
-      }
-      cudaGraph_t g = nullptr;
-      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
-      if (e != cudaSuccess) return from_cuda(e);
-      const fvh_status r = solver_step_enqueue(s, state, st);
-      e = cudaStreamEndCapture(st, &g);
-      if (r != FVH_OK) {
-        if (g) cudaGraphDestroy(g);
-        return r;
-      }
-      if (e != cudaSuccess) return from_cuda(e);
-      e = cudaGraphInstantiate(&s->graph, g, 0);
-      cudaGraphDestroy(g);
-      if (e != cudaSuccess) {
-        s->graph = nullptr;
-        return from_cuda(e);
-      }
-      s->graph_stream = st;
-      s->graph_state = *state;
-    }
-    return from_cuda(cudaGraphLaunch(s->graph, st));
-  }
-  return solver_step_enqueue(s, state, st);
+  return solver_step_flags(s, state, cs(stream), fvh::mixed::step_flags());
 }
 
 fvh_status fvh_solver_check(fvh_solver *s, fvh_stream_t stream, double *soln_time,
@@ -610,7 +648,8 @@ fvh_status fvh_solver_run(fvh_solver *s, const fvh_state_view *state, int64_t ns
     const int64_t chunk = stop_at_final_time
                               ? (nsteps - n < check_every ? nsteps - n : check_every)
                               : nsteps - n;
-    for (int64_t k = 0; k < chunk && r == FVH_OK; ++k, ++n) r = fvh_solver_step(s, state, stream);
+    for (int64_t k = 0; k < chunk && r == FVH_OK; ++k, ++n)
+      r = solver_step_flags(s, state, cs(stream), chunk_flags(k, chunk));
     if (r != FVH_OK) break;
   }
   if (r == FVH_OK) r = fvh_solver_check(s, stream, nullptr, nullptr);

@@ -75,7 +75,8 @@ struct workspace {
   // first W_CV vertices, [(k * D + i) * nc + c]: a warp's 32 consecutive cells
   // read 32 consecutive words, with no dependent index load
   float *ell_vdx = nullptr;
-  unsigned *ticket = nullptr;  // blocks of pack_dt done (the last one computes dt)
+  unsigned *ticket = nullptr;  // blocks done (the last one computes dt)
+  unsigned *dtinv_max = nullptr;  // corrector's CFL maximum for the next step (FP32 bits)
 };
 
 __device__ __forceinline__ void stg256(float4 *p, float4 a, float4 b) {
@@ -391,33 +392,56 @@ __device__ __forceinline__ float block_max_f(float v) {
 // ---------------------------------------------------------------------------
 // pack + dt partial maxima
 // ---------------------------------------------------------------------------
+// max over the faces of c of (a + |v.n|) A/V in FP32 (tasks.h:349-360)
+template <int D>
+__device__ __forceinline__ float cell_cfl(const fvh_mesh_view &m, const workspace &w, int c,
+                                          const float *v, float a) {
+  const float iv = w.inv_vol32[c];
+  float r = 0.f;
+  const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
+  for (int k = 0; k < nq; ++k) {
+    int f = m.cell_faces[q0 + k];
+    f = f < 0 ? ~f : f;
+    float n[D], area;
+    face_geo<D>(w, f, n, area);
+    r = smax((a + fabsf(phys::dot<float, D>(v, n))) * (area * iv), r);
+  }
+  return r;
+}
+
+// dt = min(CFL / max, t_f - t) from the maximum, in FP64 (tasks.h:362-375)
+__device__ __forceinline__ void finish_dt(double dt_inv, double cfl, double final_time,
+                                          const double *soln_time, double *dt_out,
+                                          fvh_device_status *status) {
+  const double max_dt = final_time - soln_time[0];
+  if (dt_inv <= 0) {
+    atomicMin(status, status_key(0, FVH_ERR_INFINITE_DT));
+    dt_out[0] = 0;
+  } else {
+    double time_step = 1 / dt_inv;
+    time_step *= cfl;
+    dt_out[0] = smin(time_step, max_dt);
+  }
+}
 // Also computes dt: every block publishes its maximum and the last block to
 // finish (a ticket counter, reset by that block) reduces them in FP64.
 template <int D>
 __global__ void __launch_bounds__(kDtThreads)
 pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, double *partial,
                const fvh_params p, const double *soln_time, double *dt_out,
-               fvh_device_status *status) {
+               fvh_device_status *status, int rev) {
   // writes w.pack, the input of the predictor
   float dt_inv = 0.f;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.num_cells;
-       c += gridDim.x * blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.num_cells;
+       i += gridDim.x * blockDim.x) {
+    const int c = rev ? m.num_cells - 1 - i : i;
     float v[D];
 #pragma unroll
     for (int i = 0; i < D; ++i) v[i] = d2f(s.velocity[i][c]);
     const float a = d2f(s.sound_speed[c]);
     store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
                   d2f(s.internal_energy[c]), a);
-    const float iv = w.inv_vol32[c];
-    const int q0 = m.cell_face_offsets[c], nq = m.cell_face_offsets[c + 1] - q0;
-    for (int k = 0; k < nq; ++k) {
-      int f = m.cell_faces[q0 + k];
-      f = f < 0 ? ~f : f;
-      float n[D], area;
-      face_geo<D>(w, f, n, area);
-      const float dti = (a + fabsf(phys::dot<float, D>(v, n))) * (area * iv);
-      dt_inv = smax(dti, dt_inv);
-    }
+    dt_inv = smax(cell_cfl<D>(m, w, c, v, a), dt_inv);
   }
   dt_inv = block_max_f(dt_inv);
   __shared__ bool last;
@@ -435,15 +459,7 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
   v = block_max(v);
   if (threadIdx.x == 0) {
     *w.ticket = 0u;
-    const double max_dt = p.final_time - soln_time[0];
-    if (v <= 0) {
-      atomicMin(status, status_key(0, FVH_ERR_INFINITE_DT));
-      dt_out[0] = 0;
-    } else {
-      double time_step = 1 / v;
-      time_step *= p.cfl;
-      dt_out[0] = smin(time_step, max_dt);
-    }
+    finish_dt(v, p.cfl, p.final_time, soln_time, dt_out, status);
   }
 }
 
@@ -455,13 +471,14 @@ pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, doubl
 template <int D>
 __global__ void __launch_bounds__(kDtThreads)
 pack_dt_batch_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
-                     const problem_map pm) {
+                     const problem_map pm, int rev) {
   __shared__ int block_pr[kDtThreads / 32];
   __shared__ float block_v[kDtThreads / 32];
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = rev ? m.num_cells - 1 - i : i;
   float dti_c = 0.f;
   int pr = -1;
-  if (c < m.num_cells) {
+  if (i < m.num_cells) {
     pr = pm.cell_problem[c];
     float v[D];
 #pragma unroll
@@ -671,8 +688,9 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
 // registers there, 64 in 2D.
 template <int D, bool LIMIT, int BS>
 __global__ void __launch_bounds__(BS, (D == 2 ? 1024 : 512) / BS)
-gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk) {
-  for (int c0 = blockIdx.x * BS + threadIdx.x; c0 < m.num_cells; c0 += gridDim.x * BS) {
+gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk, int rev) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_cells; i += gridDim.x * BS) {
+    const int c0 = rev ? m.num_cells - 1 - i : i;
     float xh[3], xl[3], u0[D + 4];
     load_cen<D>(w.ccen, c0, xh, xl);
     pack_values<D>(load_pack<D>(pk, c0), u0);
@@ -785,11 +803,16 @@ __device__ __forceinline__ bool negative(double x) {
 // so every FP64 value takes one double-float increment per time step and
 // keeps all of its bits.  FP64 pipe per step: 2D+5 additions (the splits run
 // on the integer pipe).
+//
+// pk_out: the predictor's output pack; for the corrector (when not null) the
+// pack of the next step, equal to what pack_dt writes from the new FP64 state,
+// with the FP32 velocity and sound speed also returned in vnext / anext.
 template <int D, int STAGE>
 __device__ __forceinline__ void cell_update(const fvh_state_view &s, const workspace &w,
                                             float4 *__restrict__ pk_out, const problem_map &pm,
                                             int c, int pr, df dts, const float *shi,
-                                            const float *slo, const update_consts &k) {
+                                            const float *slo, const update_consts &k,
+                                            float *vnext = nullptr, float *anext = nullptr) {
   constexpr int L4 = layout<D>::DEL4;
   const df scale = df_mul(dts, {w.inv_vol32[c], w.inv_vol_lo[c]});
   df du[D + 2];
@@ -885,9 +908,58 @@ __device__ __forceinline__ void cell_update(const fvh_state_view &s, const works
     s.pressure[c] = p;
     s.temperature[c] = k.unit_cv ? en : en * k.inv_cv;
     s.sound_speed[c] = f2d(a);
+    if (pk_out) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) vnext[i] = d2f(vel[i]);
+      *anext = a;
+      store_pack<D>(pk_out, c, d2f(mass), vnext, d2f(p), d2f(en), a);
+    }
     if (negative(en) || negative(mass))
       atomicMin(&pm.status[pr], status_key(c, FVH_ERR_NEGATIVE_STATE));
   }
+}
+
+constexpr int kCflMaxBlocks = 1216;
+
+// The corrector's dt for the next step: the CFL maximum of the cells' new
+// state, one integer atomicMax per block on the FP32 bits (order-independent),
+// and the last block to finish computes dt as pack_dt would.
+struct next_dt {
+  double cfl = 0, final_time = 0;
+  const double *soln_time = nullptr;
+  double *dt = nullptr;
+  fvh_device_status *status = nullptr;
+  bool write_next = false;  // the corrector writes the next step's pack and dt
+};
+
+__device__ __forceinline__ void finish_cfl(const workspace &w, const next_dt &nd, float dt_inv) {
+  dt_inv = block_max_f(dt_inv);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    atomicMax(w.dtinv_max, __float_as_uint(dt_inv));
+    __threadfence();
+    last = atomicAdd(w.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    const float mx = __uint_as_float(atomicExch(w.dtinv_max, 0u));
+    *w.ticket = 0u;
+    finish_dt(f2d(mx), nd.cfl, nd.final_time, nd.soln_time, nd.dt, nd.status);
+  }
+}
+
+// CFL maximum of a cell the corrector leaves untouched (its problem is at its
+// final time): from its current pack record.
+template <int D>
+__device__ __forceinline__ float untouched_cfl(const fvh_mesh_view &m, const workspace &w,
+                                               int c) {
+  const float4 a = w.pack[2 * (size_t)c], b = w.pack[2 * (size_t)c + 1];
+  float v[D];
+  v[0] = a.y;
+  v[1] = a.z;
+  if (D == 3) v[D - 1] = a.w;
+  return cell_cfl<D>(m, w, c, v, D == 2 ? b.y : b.z);
 }
 
 // Per-thread cache of the stage's dt for the problem of the current cell; the
@@ -913,17 +985,24 @@ struct stage_dt {
 };
 
 // Cell-centric schedule: each cell evaluates the fluxes of its own faces.
-template <int D, int KIND, bool SECOND, int BS, int STAGE>
+// NEXT (corrector): 0 = nothing more, 2 = the next step's pack and dt.
+template <int D, int KIND, bool SECOND, int BS, int STAGE, int NEXT = 0>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                    const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out,
-                   const problem_map pm, const update_consts uc, int swap, int outflow) {
+                   const problem_map pm, const update_consts uc, int swap, int outflow,
+                   int rev, const next_dt nd) {
   // Reads pk_in (all cells) and the cell's own FP64 state; the predictor writes
   // the cell's increments and pk_out record, the corrector its FP64 state.
   stage_dt sdt;
-  for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
+  float dt_inv = 0.f;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_cells; i += gridDim.x * BS) {
+    const int c = rev ? m.num_cells - 1 - i : i;
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    if (!sdt.at(pm, c, pr, uc.factor)) continue;
+    if (!sdt.at(pm, c, pr, uc.factor)) {
+      if (NEXT == 2) dt_inv = smax(untouched_cfl<D>(m, w, c), dt_inv);
+      continue;
+    }
     // face sums in FP32 with error-free two-sum compensation (hi + lo carries
     // about 48 bits)
     float shi[D + 2], slo[D + 2];
@@ -938,17 +1017,21 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc);
+    float vn[D], an;
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an);
+    if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
   }
+  if (NEXT == 2) finish_cfl(w, nd, dt_inv);
 }
 
 // Face schedule, part 1: one flux per face into the FP32 face-flux array.
 template <int D, int KIND, bool SECOND, int BS>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 face_flux_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk_in, int swap,
-                 int outflow) {
+                 int outflow, int rev) {
   constexpr int F4 = layout<D>::FLUX4;
-  for (int f = blockIdx.x * BS + threadIdx.x; f < m.num_faces; f += gridDim.x * BS) {
+  for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_faces; i += gridDim.x * BS) {
+    const int f = rev ? m.num_faces - 1 - i : i;
     float F[4 * F4];
     face_flux_area<D, KIND, SECOND>(m, w, pk_in, f, swap, outflow, F);
 #pragma unroll
@@ -960,16 +1043,21 @@ face_flux_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 }
 
 // Face schedule, part 2: cell-centric gather of the face-flux array + update.
-template <int D, int BS, int STAGE>
+template <int D, int BS, int STAGE, int NEXT = 0>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                      float4 *__restrict__ pk_out, const problem_map pm,
-                     const update_consts uc) {
+                     const update_consts uc, int rev, const next_dt nd) {
   constexpr int F4 = layout<D>::FLUX4;
   stage_dt sdt;
-  for (int c = blockIdx.x * BS + threadIdx.x; c < m.num_cells; c += gridDim.x * BS) {
+  float dt_inv = 0.f;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_cells; i += gridDim.x * BS) {
+    const int c = rev ? m.num_cells - 1 - i : i;
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
-    if (!sdt.at(pm, c, pr, uc.factor)) continue;
+    if (!sdt.at(pm, c, pr, uc.factor)) {
+      if (NEXT == 2) dt_inv = smax(untouched_cfl<D>(m, w, c), dt_inv);
+      continue;
+    }
     float shi[D + 2], slo[D + 2];
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) shi[k] = slo[k] = 0.f;
@@ -989,8 +1077,11 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
 #pragma unroll
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
-    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc);
+    float vn[D], an;
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an);
+    if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
   }
+  if (NEXT == 2) finish_cfl(w, nd, dt_inv);
 }
 
 // Diagnostic: the integer-pipe conversions applied to an array, so they can be
@@ -1025,7 +1116,7 @@ static size_t bytes_for(int nc, int nf, int nv) {
                            (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4) + (size_t)nc * L::DEL4) +
          2 * sizeof(float) * (size_t)nc +
          sizeof(float) * (size_t)nc * L::W_CV * D +
-         256 * 16;  // alignment of each carved array + the ticket
+         256 * 18;  // alignment of each carved array + counters
 }
 
 template <int D>
@@ -1050,6 +1141,7 @@ static void carve(workspace *w) {
   w->inv_vol_lo = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
   w->ell_vdx = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc * L::W_CV * D));
   w->ticket = reinterpret_cast<unsigned *>(take(256));
+  w->dtinv_max = reinterpret_cast<unsigned *>(take(256));
 }
 
 template <int D>
@@ -1116,18 +1208,29 @@ void destroy(workspace *w) {
 }
 
 template <int D, int KIND, bool SECOND, int BS>
+// dir: traversal direction of the previous launch; each launch runs the other
+// way, so it starts on the cells/faces its predecessor touched last (still in
+// L2).  Results do not depend on the order.
 static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                             const fvh_state_view &s, const problem_map &pm, int stage,
-                            int cpt, int schedule, cudaStream_t st, const launch_mark &mark) {
+                            int cpt, int schedule, cudaStream_t st, const launch_mark &mark,
+                            int &dir, const next_dt *nd) {
   const long long per = (long long)BS * cpt;
   const int nb = (int)((m.num_cells + per - 1) / per);
   const float4 *pk_in = stage == 0 ? w->pack : w->pack2;
-  float4 *pk_out = stage == 0 ? w->pack2 : nullptr;
+  // nd is given for a single mesh (the batch has per-problem dt kernels)
+  const bool next = stage == 1 && nd != nullptr && nd->write_next;
+  float4 *pk_out = stage == 0 ? w->pack2 : next ? w->pack : nullptr;
+  const next_dt ndv = nd ? *nd : next_dt();
+  // a corrector that finishes dt ends with one same-address atomic pair per
+  // block: at most kCflMaxBlocks blocks (grid-stride)
+  const int nb_next = nb < kCflMaxBlocks ? nb : kCflMaxBlocks;
   if (SECOND) {
+    dir ^= 1;
     if (p.limiter == FVH_LIMITER_NONE)
-      gradients_kernel<D, false, BS><<<nb, BS, 0, st>>>(m, *w, pk_in);
+      gradients_kernel<D, false, BS><<<nb, BS, 0, st>>>(m, *w, pk_in, dir);
     else
-      gradients_kernel<D, true, BS><<<nb, BS, 0, st>>>(m, *w, pk_in);
+      gradients_kernel<D, true, BS><<<nb, BS, 0, st>>>(m, *w, pk_in, dir);
     mark("gradients");
   }
   update_consts k;
@@ -1140,21 +1243,30 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
   k.unit_cv = p.cv == 1.0;
   if (schedule == 1) {
     const int nbf = (int)((m.num_faces + per - 1) / per);
+    dir ^= 1;
     face_flux_kernel<D, KIND, SECOND, BS><<<nbf, BS, 0, st>>>(m, *w, pk_in, p.recon_swap_ep,
-                                                               p.boundary);
+                                                               p.boundary, dir);
     mark("face_flux");
+    dir ^= 1;
     if (stage == 0)
-      gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
+      gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv);
+    else if (next)
+      gather_update_kernel<D, BS, 1, 2><<<nb_next, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir,
+                                                                 ndv);
     else
-      gather_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k);
+      gather_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv);
     mark("gather_update");
   } else {
+    dir ^= 1;
     if (stage == 0)
       flux_update_kernel<D, KIND, SECOND, BS, 0><<<nb, BS, 0, st>>>(
-          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
+    else if (next)
+      flux_update_kernel<D, KIND, SECOND, BS, 1, 2><<<nb_next, BS, 0, st>>>(
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
     else
       flux_update_kernel<D, KIND, SECOND, BS, 1><<<nb, BS, 0, st>>>(
-          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary);
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
     mark("flux_update");
   }
 }
@@ -1162,36 +1274,39 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
 template <int D, int KIND, bool SECOND>
 static void launch_stage(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                          const fvh_state_view &s, const problem_map &pm, int stage,
-                         const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
+                         const launch_shape &sh, cudaStream_t st, const launch_mark &mark,
+                         int &dir, const next_dt *nd) {
   if (sh.block == 256)
     launch_stage_bs<D, KIND, SECOND, 256>(w, m, p, s, pm, stage, sh.cells_per_thread,
-                                          sh.schedule, st, mark);
+                                          sh.schedule, st, mark, dir, nd);
   else
     launch_stage_bs<D, KIND, SECOND, 128>(w, m, p, s, pm, stage, sh.cells_per_thread,
-                                          sh.schedule, st, mark);
+                                          sh.schedule, st, mark, dir, nd);
 }
 
 template <int D, int KIND>
 static void launch_stage_k(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                            const fvh_state_view &s, const problem_map &pm, int stage,
-                           const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
+                           const launch_shape &sh, cudaStream_t st, const launch_mark &mark,
+                           int &dir, const next_dt *nd) {
   if (p.order == 1)
-    launch_stage<D, KIND, false>(w, m, p, s, pm, stage, sh, st, mark);
+    launch_stage<D, KIND, false>(w, m, p, s, pm, stage, sh, st, mark, dir, nd);
   else
-    launch_stage<D, KIND, true>(w, m, p, s, pm, stage, sh, st, mark);
+    launch_stage<D, KIND, true>(w, m, p, s, pm, stage, sh, st, mark, dir, nd);
 }
 
 template <int D>
 static void launch_stages(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                           const fvh_state_view &s, const problem_map &pm,
-                          const launch_shape &sh, cudaStream_t st, const launch_mark &mark) {
+                          const launch_shape &sh, cudaStream_t st, const launch_mark &mark,
+                          int dir, const next_dt *nd = nullptr) {
   for (int stage = 0; stage < 2; ++stage) {
     if (p.flux_kind == FVH_FLUX_RUSANOV)
-      launch_stage_k<D, FVH_FLUX_RUSANOV>(w, m, p, s, pm, stage, sh, st, mark);
+      launch_stage_k<D, FVH_FLUX_RUSANOV>(w, m, p, s, pm, stage, sh, st, mark, dir, nd);
     else if (p.flux_kind == FVH_FLUX_HLLC)
-      launch_stage_k<D, FVH_FLUX_HLLC>(w, m, p, s, pm, stage, sh, st, mark);
+      launch_stage_k<D, FVH_FLUX_HLLC>(w, m, p, s, pm, stage, sh, st, mark, dir, nd);
     else
-      launch_stage_k<D, FVH_FLUX_HLLE>(w, m, p, s, pm, stage, sh, st, mark);
+      launch_stage_k<D, FVH_FLUX_HLLE>(w, m, p, s, pm, stage, sh, st, mark, dir, nd);
   }
 }
 
@@ -1199,24 +1314,35 @@ template <int D>
 static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                           const fvh_state_view &s, double *t, double *dt, double *partial,
                           int dt_blocks, fvh_device_status *status, cudaStream_t st,
-                          const launch_mark &mark, const launch_shape &shape) {
-  pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial, p, t, dt, status);
-  mark("pack_dt");
+                          const launch_mark &mark, const launch_shape &shape,
+                          const step_flags &f) {
+  if (f.pack_first) {
+    pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial, p, t, dt, status, 0);
+    mark("pack_dt");
+  }
   problem_map pm;
   pm.dt = dt;
   pm.t = t;
   pm.status = status;
-  launch_stages<D>(w, m, p, s, pm, shape, st, mark);
+  next_dt nd;
+  nd.cfl = p.cfl;
+  nd.final_time = p.final_time;
+  nd.soln_time = t;
+  nd.dt = dt;
+  nd.status = status;
+  nd.write_next = f.write_next;
+  // pack_dt and every corrector run upwards, so the gradients start downwards
+  launch_stages<D>(w, m, p, s, pm, shape, st, mark, 0, &nd);
   return cudaGetLastError();
 }
 
 cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                  const fvh_state_view &s, double *soln_time, double *dt, double *partial,
                  int dt_blocks, fvh_device_status *status, cudaStream_t st,
-                 const launch_mark &mark, const launch_shape &shape) {
+                 const launch_mark &mark, const launch_shape &shape, step_flags f) {
   return m.dim == 2
-             ? step_d<2>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape)
-             : step_d<3>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape);
+             ? step_d<2>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape, f)
+             : step_d<3>(w, m, p, s, soln_time, dt, partial, dt_blocks, status, st, mark, shape, f);
 }
 
 template <int D>
@@ -1225,11 +1351,11 @@ static cudaError_t step_batch_d(workspace *w, const fvh_mesh_view &m, const fvh_
                                 const launch_shape &sh, cudaStream_t st,
                                 const launch_mark &mark) {
   const int nb = (m.num_cells + kDtThreads - 1) / kDtThreads;
-  pack_dt_batch_kernel<D><<<nb, kDtThreads, 0, st>>>(m, s, *w, pm);
+  pack_dt_batch_kernel<D><<<nb, kDtThreads, 0, st>>>(m, s, *w, pm, 0);
   mark("pack_dt");
   dt_final_batch_kernel<<<(pm.nproblems + 127) / 128, 128, 0, st>>>(pm, 0);
   mark("dt_final");
-  launch_stages<D>(w, m, p, s, pm, sh, st, mark);
+  launch_stages<D>(w, m, p, s, pm, sh, st, mark, 0);
   return cudaGetLastError();
 }
 
@@ -1240,9 +1366,9 @@ cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p
                     : step_batch_d<3>(w, m, p, s, pm, shape, st, mark);
 }
 
-int launches_per_step(const fvh_params &p, const launch_shape &sh) {
+int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f) {
   const int per_stage = (p.order == 1 ? 0 : 1) + (sh.schedule == 1 ? 2 : 1);
-  return 1 + 2 * per_stage;
+  return (f.pack_first ? 1 : 0) + 2 * per_stage;
 }
 
 int launches_per_step_batch(const fvh_params &p, const launch_shape &sh) {

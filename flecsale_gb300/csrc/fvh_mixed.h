@@ -44,16 +44,25 @@ constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2,
                                               {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
                                               {128, 2, 1}};
 
+// Steps of one run on a state nothing else writes in between: the corrector
+// of a step can also write the next step's FP32 pack and dt (the same bits
+// pack_dt computes from the new FP64 state), and the next step then skips
+// pack_dt.  A step with pack_first = false must follow one with write_next.
+struct step_flags {
+  bool pack_first = true;   // run pack_dt (the pack and dt from the FP64 state)
+  bool write_next = false;  // the corrector writes the next step's pack and dt
+};
+
 // One full time step (dt + two half-dt stages) on the FP64 state.
 cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                  const fvh_state_view &s, double *soln_time, double *dt,
                  double *partial, int dt_blocks, fvh_device_status *status,
                  cudaStream_t st, const launch_mark &mark = launch_mark(),
-                 const launch_shape &shape = launch_shape());
+                 const launch_shape &shape = launch_shape(), step_flags f = step_flags());
 
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
-int launches_per_step(const fvh_params &p, const launch_shape &sh);
+int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags());
 int launches_per_step_batch(const fvh_params &p, const launch_shape &sh);
 
 // Independent problems concatenated into one mesh: problem k owns the cells

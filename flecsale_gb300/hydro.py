@@ -136,6 +136,7 @@ def _declare(L: C.CDLL) -> None:
                                               C.POINTER(C.c_double), vp]),
         "fvh_solver_launches_per_step": (C.c_int32, [vp]),
         "fvh_solver_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
+        "fvh_solver_launches_per_run": (C.c_int64, [vp, C.c_int64]),
         "fvh_debug_split": (C.c_int, [vp, C.c_int64, vp, vp, vp, vp, vp]),
         "fvh_input_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
         "fvh_input_load_string": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
@@ -466,7 +467,8 @@ class Solver:
                 "ms_per_step": ms.value}
 
     def profile(self, state: DeviceState, nsteps: int, stream=None) -> dict:
-        """{kernel name: (mean ms per launch, launches per step)}."""
+        """{kernel name: (mean ms per launch, launches per step)} over nsteps steps
+        launched as a run launches them."""
         mx = 16
         names = (C.c_char_p * mx)()
         ms = np.zeros(mx)
@@ -474,7 +476,10 @@ class Solver:
         nk = C.c_int32()
         check(lib().fvh_solver_profile(self._h, C.byref(state.view), nsteps, mx, names, _dptr(ms),
                                        per, C.byref(nk), stream_handle(stream)), "fvh_solver_profile")
-        return {names[k].decode(): (float(ms[k]), int(per[k])) for k in range(nk.value)}
+        return {names[k].decode(): (float(ms[k]), per[k] / nsteps) for k in range(nk.value)}
+
+    def launches_per_run(self, nsteps: int) -> int:
+        return lib().fvh_solver_launches_per_run(self._h, nsteps)
 
     @property
     def d_soln_time(self) -> int:

@@ -261,7 +261,10 @@ fvh_status fvh_solver_step(fvh_solver *s, const fvh_state_view *state,
 
 /* nsteps steps, stream-ordered.  With stop_at_final_time != 0 the host checks the
  * solution time every check_every steps and stops once it reaches final_time
- * (the dt clamp of tasks.h:373 makes the last step land on it). */
+ * (the dt clamp of tasks.h:373 makes the last step land on it).  Within a run
+ * (between host checks) the state must not be written by anyone else: in the
+ * mixed form a step's corrector prepares the next step's FP32 pack and dt.
+ * Results are bitwise those of the same number of fvh_solver_step calls. */
 fvh_status fvh_solver_run(fvh_solver *s, const fvh_state_view *state,
                           int64_t nsteps, int32_t stop_at_final_time,
                           int32_t check_every, int64_t *steps_done,
@@ -300,14 +303,20 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
                                int32_t *block, int32_t *cells_per_thread, int32_t *schedule,
                                double *best_ms_per_step, fvh_stream_t stream);
 
-/* Profiling run: nsteps steps launched kernel by kernel with a CUDA event
- * recorded on the stream after every launch.  For each distinct kernel name
- * (at most max_kernels) returns its static name, its mean duration in
- * milliseconds per launch and its launches per step.  Synchronises. */
+/* Kernel launches of fvh_solver_run(s, state, nsteps, 0, ...): in the mixed
+ * form the first step computes the FP32 pack and dt from the FP64 state and
+ * every later step gets them from the previous step's corrector. */
+int64_t fvh_solver_launches_per_run(const fvh_solver *s, int64_t nsteps);
+
+/* Profiling run: nsteps steps, launched as fvh_solver_run launches them but
+ * kernel by kernel, with a CUDA event recorded on the stream after every
+ * launch.  For each distinct kernel name (at most max_kernels) returns its
+ * static name, its mean duration in milliseconds per launch and its number of
+ * launches in the nsteps steps.  Synchronises. */
 fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state,
                               int32_t nsteps, int32_t max_kernels,
                               const char **names, double *mean_ms,
-                              int32_t *launches_per_step, int32_t *nkernels,
+                              int32_t *launches, int32_t *nkernels,
                               fvh_stream_t stream);
 
 /* Synchronises the stream, reads the status word and the solution time. */

@@ -180,3 +180,41 @@ def test_integer_pipe_conversions_exact(cuda):
     H.check(H.lib().fvh_debug_split(xd.data_ptr(), 1, h1.data_ptr(), l1.data_ptr(),
                                     r1.data_ptr(), b1.data_ptr(), None), "fvh_debug_split")
     assert np.isnan(r1.cpu().numpy()[0]) and np.isnan(h1.cpu().numpy()[0])
+
+
+@pytest.mark.parametrize("dim,schedule,final_time", [(2, 0, 10.0), (2, 1, 10.0), (3, 1, 10.0),
+                                                     (2, 1, 0.02)])
+def test_run_equals_single_steps_bitwise(cuda, dim, schedule, final_time):
+    """Inside fvh_solver_run each corrector prepares the next step's FP32 pack
+    and dt; the result must be bitwise that of the same number of single
+    steps (each recomputing pack and dt from the FP64 state), also when the
+    run passes the final time (dt = 0 steps leave the state untouched)."""
+    torch = cuda
+    n = (96, 80) if dim == 2 else (16, 14, 12)
+    mesh = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, 0.2, 6)
+    p = H.make_params(dim, flux="hllc", cfl=0.4 if dim == 2 else 0.3, precision="mixed",
+                      boundary="outflow", final_time=final_time)
+    s0 = H.initial_state("four_quadrant" if dim == 2 else "inner_cube", mesh, p, seed=4)
+    dmesh = H.DeviceMesh(mesh)
+    stream = torch.cuda.Stream()
+    out = []
+    for mode in ("run", "steps", "run_default_stream"):
+        ds = H.DeviceState(dim, mesh.num_cells)
+        sol = H.Solver(dmesh, p)
+        sol.set_shape(128, 1, schedule)
+        st = None if mode == "run_default_stream" else stream
+        ds.upload(s0, st)
+        sol.reset(0.0, st)
+        if mode == "steps":
+            for _ in range(25):
+                sol.step(ds, st)
+        else:
+            sol.run(ds, 25, stream=st)
+        code, t, _ = sol.status(st)
+        assert code == 0
+        out.append((ds.download(st), t))
+    for s, t in out[1:]:
+        assert t == out[0][1]
+        assert np.array_equal(s, out[0][0])
+    if final_time < 1:
+        assert out[0][1] == final_time
