@@ -367,11 +367,12 @@ def run_3d(torch, stream, n: int = 192, steps: int = 100) -> dict:
         sv = H.Solver(dm, p)
         ds.upload(s0, stream)
         sv.reset(0.0, stream)
+        if form == "mixed":
+            out["mixed_launch_shape"] = sv.autotune(ds, 3, stream)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
-            sv.step(ds, stream)
+        sv.run(ds, steps, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)

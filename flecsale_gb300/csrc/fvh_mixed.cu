@@ -156,7 +156,8 @@ __device__ __forceinline__ void load_cen(const float4 *cc, int c, float *hi, flo
     const float4 t = cc[c];
     hi[0] = t.x; hi[1] = t.y; lo[0] = t.z; lo[1] = t.w;
   } else {
-    const float4 a = cc[2 * (size_t)c], b = cc[2 * (size_t)c + 1];
+    float4 a, b;
+    ldg256(cc + 2 * (size_t)c, a, b);  // hi and lo float4 in one 32-byte record
     hi[0] = a.x; hi[1] = a.y; hi[D - 1] = a.z;
     lo[0] = b.x; lo[1] = b.y; lo[D - 1] = b.z;
   }
