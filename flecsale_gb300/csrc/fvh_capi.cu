@@ -816,6 +816,38 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
   cudaError_t e = cudaMemcpyAsync(s->scalars, s->host_scalars + 1, sizeof(double),
                                   cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return from_cuda(e);
+  // Pinned (device-mapped) host planes and the mixed form: the first pack_dt
+  // reads the state straight from host memory (storing it into the device
+  // state as it goes) and the last corrector writes the new state back to host
+  // memory while it computes, so the transfers overlap the kernels instead of
+  // preceding and following them.
+  cudaPointerAttributes attr{};
+  if (nsteps > 0 && s->params.precision == FVH_PRECISION_MIXED &&
+      cudaPointerGetAttributes(&attr, host_planes) == cudaSuccess &&
+      attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+    double *hp = static_cast<double *>(attr.devicePointer);
+    fvh_state_view hv{};
+    int k = 0;
+    hv.density = hp + (size_t)k++ * nc;
+    for (int d = 0; d < D; ++d) hv.velocity[d] = hp + (size_t)k++ * nc;
+    hv.internal_energy = hp + (size_t)k++ * nc;
+    hv.pressure = hp + (size_t)k++ * nc;
+    hv.temperature = hp + (size_t)k++ * nc;
+    hv.sound_speed = hp + (size_t)k++ * nc;
+    fvh_status r = FVH_OK;
+    for (int64_t n = 0; n < nsteps && r == FVH_OK; ++n) {
+      fvh::mixed::step_flags f = chunk_flags(n, nsteps);
+      if (n == 0) f.src = &hv;
+      if (n + 1 == nsteps) f.out = &hv;
+      r = solver_step_enqueue(s, dev_state, st, {}, f);
+    }
+    if (r != FVH_OK) return r;
+    double t = 0;
+    r = fvh_solver_check(s, stream, &t, nullptr);
+    *soln_time = t;
+    return r;
+  }
+  cudaGetLastError();  // a pageable pointer is not an error
   fvh_status r = fvh_state_upload(dev_state, D, nc, host_planes, stream);
   for (int64_t k = 0; k < nsteps && r == FVH_OK; ++k) r = fvh_solver_step(s, dev_state, stream);
   if (r == FVH_OK) r = fvh_state_download(dev_state, D, nc, host_planes, stream);

@@ -430,18 +430,32 @@ template <int D>
 __global__ void __launch_bounds__(kDtThreads)
 pack_dt_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w, double *partial,
                const fvh_params p, const double *soln_time, double *dt_out,
-               fvh_device_status *status, int rev) {
-  // writes w.pack, the input of the predictor
+               fvh_device_status *status, int rev, const fvh_state_view src, int copy) {
+  // writes w.pack, the input of the predictor; with copy, the state is read
+  // from src (host memory) and stored into s on the way (T is not an input)
   float dt_inv = 0.f;
+  const fvh_state_view &in = copy ? src : s;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m.num_cells;
        i += gridDim.x * blockDim.x) {
     const int c = rev ? m.num_cells - 1 - i : i;
+    double vd[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) vd[i] = in.velocity[i][c];
+    const double dd = in.density[c], ed = in.internal_energy[c], pd = in.pressure[c],
+                 ad = in.sound_speed[c];
+    if (copy) {
+      s.density[c] = dd;
+#pragma unroll
+      for (int i = 0; i < D; ++i) s.velocity[i][c] = vd[i];
+      s.internal_energy[c] = ed;
+      s.pressure[c] = pd;
+      s.sound_speed[c] = ad;
+    }
     float v[D];
 #pragma unroll
-    for (int i = 0; i < D; ++i) v[i] = d2f(s.velocity[i][c]);
-    const float a = d2f(s.sound_speed[c]);
-    store_pack<D>(w.pack, c, d2f(s.density[c]), v, d2f(s.pressure[c]),
-                  d2f(s.internal_energy[c]), a);
+    for (int i = 0; i < D; ++i) v[i] = d2f(vd[i]);
+    const float a = d2f(ad);
+    store_pack<D>(w.pack, c, d2f(dd), v, d2f(pd), d2f(ed), a);
     dt_inv = smax(cell_cfl<D>(m, w, c, v, a), dt_inv);
   }
   dt_inv = block_max_f(dt_inv);
@@ -813,7 +827,8 @@ __device__ __forceinline__ void cell_update(const fvh_state_view &s, const works
                                             float4 *__restrict__ pk_out, const problem_map &pm,
                                             int c, int pr, df dts, const float *shi,
                                             const float *slo, const update_consts &k,
-                                            float *vnext = nullptr, float *anext = nullptr) {
+                                            float *vnext = nullptr, float *anext = nullptr,
+                                            const fvh_state_view *out = nullptr) {
   constexpr int L4 = layout<D>::DEL4;
   const df scale = df_mul(dts, {w.inv_vol32[c], w.inv_vol_lo[c]});
   df du[D + 2];
@@ -909,6 +924,15 @@ __device__ __forceinline__ void cell_update(const fvh_state_view &s, const works
     s.pressure[c] = p;
     s.temperature[c] = k.unit_cv ? en : en * k.inv_cv;
     s.sound_speed[c] = f2d(a);
+    if (out) {  // the caller's copy of the state (host memory)
+      out->density[c] = mass;
+#pragma unroll
+      for (int i = 0; i < D; ++i) out->velocity[i][c] = vel[i];
+      out->internal_energy[c] = en;
+      out->pressure[c] = p;
+      out->temperature[c] = k.unit_cv ? en : en * k.inv_cv;
+      out->sound_speed[c] = f2d(a);
+    }
     if (pk_out) {
 #pragma unroll
       for (int i = 0; i < D; ++i) vnext[i] = d2f(vel[i]);
@@ -931,6 +955,8 @@ struct next_dt {
   double *dt = nullptr;
   fvh_device_status *status = nullptr;
   bool write_next = false;  // the corrector writes the next step's pack and dt
+  fvh_state_view out{};     // with has_out, the corrector also writes the state here
+  int has_out = 0;
 };
 
 __device__ __forceinline__ void finish_cfl(const workspace &w, const next_dt &nd, float dt_inv) {
@@ -992,7 +1018,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                    const float4 *__restrict__ pk_in, float4 *__restrict__ pk_out,
                    const problem_map pm, const update_consts uc, int swap, int outflow,
-                   int rev, const next_dt nd) {
+                   int rev, const next_dt nd, const fvh_state_view out, int has_out) {
   // Reads pk_in (all cells) and the cell's own FP64 state; the predictor writes
   // the cell's increments and pk_out record, the corrector its FP64 state.
   stage_dt sdt;
@@ -1019,7 +1045,8 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
     float vn[D], an;
-    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an);
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an,
+                          STAGE == 1 && has_out ? &out : nullptr);
     if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
   }
   if (NEXT == 2) finish_cfl(w, nd, dt_inv);
@@ -1048,7 +1075,8 @@ template <int D, int BS, int STAGE, int NEXT = 0>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
                      float4 *__restrict__ pk_out, const problem_map pm,
-                     const update_consts uc, int rev, const next_dt nd) {
+                     const update_consts uc, int rev, const next_dt nd,
+                     const fvh_state_view out, int has_out) {
   constexpr int F4 = layout<D>::FLUX4;
   stage_dt sdt;
   float dt_inv = 0.f;
@@ -1079,7 +1107,8 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
       for (int k = 0; k < D + 2; ++k) two_sum_acc(shi[k], slo[k], sf >= 0 ? -F[k] : F[k]);
     }
     float vn[D], an;
-    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an);
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an,
+                          STAGE == 1 && has_out ? &out : nullptr);
     if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
   }
   if (NEXT == 2) finish_cfl(w, nd, dt_inv);
@@ -1250,24 +1279,28 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
     mark("face_flux");
     dir ^= 1;
     if (stage == 0)
-      gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv);
+      gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
+                                                        ndv.out, 0);
     else if (next)
       gather_update_kernel<D, BS, 1, 2><<<nb_next, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir,
-                                                                 ndv);
+                                                                 ndv, ndv.out, ndv.has_out);
     else
-      gather_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv);
+      gather_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
+                                                        ndv.out, ndv.has_out);
     mark("gather_update");
   } else {
     dir ^= 1;
     if (stage == 0)
       flux_update_kernel<D, KIND, SECOND, BS, 0><<<nb, BS, 0, st>>>(
-          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out, 0);
     else if (next)
       flux_update_kernel<D, KIND, SECOND, BS, 1, 2><<<nb_next, BS, 0, st>>>(
-          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out,
+          ndv.has_out);
     else
       flux_update_kernel<D, KIND, SECOND, BS, 1><<<nb, BS, 0, st>>>(
-          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv);
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out,
+          ndv.has_out);
     mark("flux_update");
   }
 }
@@ -1318,7 +1351,8 @@ static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params
                           const launch_mark &mark, const launch_shape &shape,
                           const step_flags &f) {
   if (f.pack_first) {
-    pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial, p, t, dt, status, 0);
+    pack_dt_kernel<D><<<dt_blocks, kDtThreads, 0, st>>>(m, s, *w, partial, p, t, dt, status, 0,
+                                                         f.src ? *f.src : s, f.src ? 1 : 0);
     mark("pack_dt");
   }
   problem_map pm;
@@ -1332,6 +1366,10 @@ static cudaError_t step_d(workspace *w, const fvh_mesh_view &m, const fvh_params
   nd.dt = dt;
   nd.status = status;
   nd.write_next = f.write_next;
+  if (f.out) {
+    nd.out = *f.out;
+    nd.has_out = 1;
+  }
   // pack_dt and every corrector run upwards, so the gradients start downwards
   launch_stages<D>(w, m, p, s, pm, shape, st, mark, 0, &nd);
   return cudaGetLastError();

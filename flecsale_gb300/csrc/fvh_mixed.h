@@ -48,9 +48,15 @@ constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2,
 // of a step can also write the next step's FP32 pack and dt (the same bits
 // pack_dt computes from the new FP64 state), and the next step then skips
 // pack_dt.  A step with pack_first = false must follow one with write_next.
+//
+// src / out (optional, host-mapped views for callers holding the state in host
+// memory): pack_dt reads the state from src and stores it into the device
+// state as it packs it; the corrector also writes the new state to out.
 struct step_flags {
   bool pack_first = true;   // run pack_dt (the pack and dt from the FP64 state)
   bool write_next = false;  // the corrector writes the next step's pack and dt
+  const fvh_state_view *src = nullptr;
+  const fvh_state_view *out = nullptr;
 };
 
 // One full time step (dt + two half-dt stages) on the FP64 state.

@@ -218,3 +218,39 @@ def test_run_equals_single_steps_bitwise(cuda, dim, schedule, final_time):
         assert np.array_equal(s, out[0][0])
     if final_time < 1:
         assert out[0][1] == final_time
+
+
+@pytest.mark.parametrize("nsteps", [1, 4])
+def test_advance_host_pinned_equals_copies(cuda, nsteps):
+    """fvh_solver_advance_host with pinned host planes (kernels read and write
+    host memory directly) gives the same bits as with pageable planes (copies)
+    and as upload + run + download; the device state ends up the same too."""
+    torch = cuda
+    mesh = H.HostMesh.box(2, (120, 100), [0, 0], [1, 1], 0.2, 9)
+    p = H.make_params(2, flux="hllc", cfl=0.4, precision="mixed", boundary="outflow")
+    s0 = H.initial_state("four_quadrant", mesh, p, seed=1)
+    dmesh = H.DeviceMesh(mesh)
+    stream = torch.cuda.Stream()
+    nc = mesh.num_cells
+    res = []
+    for kind in ("pinned", "pageable", "run"):
+        ds = H.DeviceState(2, nc)
+        sol = H.Solver(dmesh, p)
+        if kind == "run":
+            ds.upload(s0, stream)
+            sol.reset(0.125, stream)
+            sol.run(ds, nsteps, stream=stream)
+            host, t = ds.download(stream), sol.soln_time(stream)
+        else:
+            if kind == "pinned":
+                host = torch.empty((7, nc), dtype=torch.float64, pin_memory=True).numpy()
+            else:
+                host = np.empty((7, nc), np.float64)
+            host[:] = s0[:7]
+            t = sol.advance_host(ds, host, nsteps, 0.125, stream)
+        res.append((host.copy(), t, ds.download(stream)))
+    for h, t, d in res[1:]:
+        assert t == res[0][1]
+        assert np.array_equal(h, res[0][0])
+        assert np.array_equal(d, res[0][2])
+    assert not np.array_equal(res[0][0], s0[:7])
