@@ -544,10 +544,19 @@ fvh_status fvh_batch_step(fvh_batch *b, int32_t nsteps, fvh_stream_t stream) {
   if (!b || nsteps <= 0 || b->nproblems <= 0) return FVH_ERR_INVALID_ARGUMENT;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const fvh::mixed::problem_map pm = pmap(b);
+  // within one call the state is the batch's own: each corrector but the
+  // last prepares the next step's pack and per-problem CFL maxima
+  auto flags = [nsteps](int k) {
+    fvh::mixed::step_flags f;
+    f.pack_first = k == 0;
+    f.write_next = k + 1 < nsteps;
+    return f;
+  };
   if (!st) {
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < nsteps && e == cudaSuccess; ++k)
-      e = fvh::mixed::step_batch(b->ws, b->view, b->params, b->state, pm, b->shape, st);
+      e = fvh::mixed::step_batch(b->ws, b->view, b->params, b->state, pm, b->shape, st, {},
+                                 flags(k));
     return from_cuda(e);
   }
   if (b->graph_stream != st) {
@@ -561,7 +570,8 @@ fvh_status fvh_batch_step(fvh_batch *b, int32_t nsteps, fvh_stream_t stream) {
     if (e != cudaSuccess) return from_cuda(e);
     cudaError_t le = cudaSuccess;
     for (int k = 0; k < nsteps && le == cudaSuccess; ++k)
-      le = fvh::mixed::step_batch(b->ws, b->view, b->params, b->state, pm, b->shape, st);
+      le = fvh::mixed::step_batch(b->ws, b->view, b->params, b->state, pm, b->shape, st, {},
+                                  flags(k));
     e = cudaStreamEndCapture(st, &g);
     if (le != cudaSuccess || e != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -738,7 +748,11 @@ fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cac
 int32_t fvh_batch_num_problems(const fvh_batch *b) { return b ? b->nproblems : 0; }
 int64_t fvh_batch_num_cells(const fvh_batch *b) { return b ? b->view.num_cells : 0; }
 int32_t fvh_batch_launches_per_step(const fvh_batch *b) {
-  return b ? fvh::mixed::launches_per_step_batch(b->params, b->shape) : 0;
+  if (!b) return 0;
+  fvh::mixed::step_flags f;  // a step after the first of a call
+  f.pack_first = false;
+  f.write_next = true;
+  return fvh::mixed::launches_per_step_batch(b->params, b->shape, f);
 }
 
 }  // extern "C"

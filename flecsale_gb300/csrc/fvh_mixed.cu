@@ -957,7 +957,18 @@ struct next_dt {
   bool write_next = false;  // the corrector writes the next step's pack and dt
   fvh_state_view out{};     // with has_out, the corrector also writes the state here
   int has_out = 0;
+  int batch = 0;            // per-problem maxima (problem_map::dtinv_bits) instead
 };
+
+// Batch form: the next step's per-problem CFL maxima.  Lanes that arrive
+// together and share a problem combine their values; one integer atomicMax on
+// the FP32 bits per group (order-independent, as in pack_dt_batch).
+__device__ __forceinline__ void problem_cfl(const problem_map &pm, int pr, float v) {
+  const unsigned active = __activemask();
+  const unsigned grp = __match_any_sync(active, pr);
+  const unsigned mx = __reduce_max_sync(grp, __float_as_uint(v));
+  if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(&pm.dtinv_bits[pr], mx);
+}
 
 __device__ __forceinline__ void finish_cfl(const workspace &w, const next_dt &nd, float dt_inv) {
   dt_inv = block_max_f(dt_inv);
@@ -1012,7 +1023,8 @@ struct stage_dt {
 };
 
 // Cell-centric schedule: each cell evaluates the fluxes of its own faces.
-// NEXT (corrector): 0 = nothing more, 2 = the next step's pack and dt.
+// NEXT (corrector): 0 = nothing more, 2 = the next step's pack and dt, 3 = the
+// next step's pack and per-problem CFL maxima (batch).
 template <int D, int KIND, bool SECOND, int BS, int STAGE, int NEXT = 0>
 __global__ void __launch_bounds__(BS, 1024 / BS)
 flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
@@ -1028,6 +1040,7 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
     if (!sdt.at(pm, c, pr, uc.factor)) {
       if (NEXT == 2) dt_inv = smax(untouched_cfl<D>(m, w, c), dt_inv);
+      if (NEXT == 3) problem_cfl(pm, pr, untouched_cfl<D>(m, w, c));
       continue;
     }
     // face sums in FP32 with error-free two-sum compensation (hi + lo carries
@@ -1048,6 +1061,7 @@ flux_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an,
                           STAGE == 1 && has_out ? &out : nullptr);
     if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
+    if (NEXT == 3) problem_cfl(pm, pr, cell_cfl<D>(m, w, c, vn, an));
   }
   if (NEXT == 2) finish_cfl(w, nd, dt_inv);
 }
@@ -1085,6 +1099,7 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
     if (!sdt.at(pm, c, pr, uc.factor)) {
       if (NEXT == 2) dt_inv = smax(untouched_cfl<D>(m, w, c), dt_inv);
+      if (NEXT == 3) problem_cfl(pm, pr, untouched_cfl<D>(m, w, c));
       continue;
     }
     float shi[D + 2], slo[D + 2];
@@ -1110,6 +1125,7 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
     cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an,
                           STAGE == 1 && has_out ? &out : nullptr);
     if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
+    if (NEXT == 3) problem_cfl(pm, pr, cell_cfl<D>(m, w, c, vn, an));
   }
   if (NEXT == 2) finish_cfl(w, nd, dt_inv);
 }
@@ -1281,6 +1297,9 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
     if (stage == 0)
       gather_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
                                                         ndv.out, 0);
+    else if (next && ndv.batch)
+      gather_update_kernel<D, BS, 1, 3><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
+                                                           ndv.out, ndv.has_out);
     else if (next)
       gather_update_kernel<D, BS, 1, 2><<<nb_next, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir,
                                                                  ndv, ndv.out, ndv.has_out);
@@ -1293,6 +1312,10 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
     if (stage == 0)
       flux_update_kernel<D, KIND, SECOND, BS, 0><<<nb, BS, 0, st>>>(
           m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out, 0);
+    else if (next && ndv.batch)
+      flux_update_kernel<D, KIND, SECOND, BS, 1, 3><<<nb, BS, 0, st>>>(
+          m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out,
+          ndv.has_out);
     else if (next)
       flux_update_kernel<D, KIND, SECOND, BS, 1, 2><<<nb_next, BS, 0, st>>>(
           m, s, *w, pk_in, pk_out, pm, k, p.recon_swap_ep, p.boundary, dir, ndv, ndv.out,
@@ -1388,21 +1411,27 @@ template <int D>
 static cudaError_t step_batch_d(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                                 const fvh_state_view &s, const problem_map &pm,
                                 const launch_shape &sh, cudaStream_t st,
-                                const launch_mark &mark) {
-  const int nb = (m.num_cells + kDtThreads - 1) / kDtThreads;
-  pack_dt_batch_kernel<D><<<nb, kDtThreads, 0, st>>>(m, s, *w, pm, 0);
-  mark("pack_dt");
+                                const launch_mark &mark, const step_flags &f) {
+  if (f.pack_first) {
+    const int nb = (m.num_cells + kDtThreads - 1) / kDtThreads;
+    pack_dt_batch_kernel<D><<<nb, kDtThreads, 0, st>>>(m, s, *w, pm, 0);
+    mark("pack_dt");
+  }
   dt_final_batch_kernel<<<(pm.nproblems + 127) / 128, 128, 0, st>>>(pm, 0);
   mark("dt_final");
-  launch_stages<D>(w, m, p, s, pm, sh, st, mark, 0);
+  next_dt nd;
+  nd.write_next = f.write_next;
+  nd.batch = 1;
+  launch_stages<D>(w, m, p, s, pm, sh, st, mark, 0, &nd);
   return cudaGetLastError();
 }
 
 cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                        const fvh_state_view &s, const problem_map &pm,
-                       const launch_shape &shape, cudaStream_t st, const launch_mark &mark) {
-  return m.dim == 2 ? step_batch_d<2>(w, m, p, s, pm, shape, st, mark)
-                    : step_batch_d<3>(w, m, p, s, pm, shape, st, mark);
+                       const launch_shape &shape, cudaStream_t st, const launch_mark &mark,
+                       step_flags f) {
+  return m.dim == 2 ? step_batch_d<2>(w, m, p, s, pm, shape, st, mark, f)
+                    : step_batch_d<3>(w, m, p, s, pm, shape, st, mark, f);
 }
 
 int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f) {
@@ -1410,8 +1439,8 @@ int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f)
   return (f.pack_first ? 1 : 0) + 2 * per_stage;
 }
 
-int launches_per_step_batch(const fvh_params &p, const launch_shape &sh) {
-  return launches_per_step(p, sh) + 1;  // per-problem dt is a separate kernel
+int launches_per_step_batch(const fvh_params &p, const launch_shape &sh, step_flags f) {
+  return launches_per_step(p, sh, f) + 1;  // per-problem dt is a separate kernel
 }
 
 int launches_per_step(const fvh_params &p) { return launches_per_step(p, launch_shape()); }

@@ -69,7 +69,7 @@ cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
 int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags());
-int launches_per_step_batch(const fvh_params &p, const launch_shape &sh);
+int launches_per_step_batch(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags());
 
 // Independent problems concatenated into one mesh: problem k owns the cells
 // [first_cell[k], first_cell[k+1]).  All arrays are device memory.
@@ -86,10 +86,12 @@ struct problem_map {
 };
 
 // One time step of every problem of the batch (per-problem dt and time).
+// With f.write_next the corrector writes the next step's pack and per-problem
+// CFL maxima; a step with f.pack_first = false must follow such a step.
 cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                        const fvh_state_view &s, const problem_map &pm,
                        const launch_shape &shape, cudaStream_t st,
-                       const launch_mark &mark = launch_mark());
+                       const launch_mark &mark = launch_mark(), step_flags f = step_flags());
 
 // Diagnostic: hi/lo of the integer-pipe FP64 -> double-float split, the FP64
 // -> FP32 conversion and the FP32 -> FP64 conversion of hi, for x[0..n).

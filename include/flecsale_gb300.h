@@ -562,6 +562,9 @@ fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cac
 
 int32_t fvh_batch_num_problems(const fvh_batch *b);
 int64_t fvh_batch_num_cells(const fvh_batch *b);
+/* Kernel launches of a step after the first of one fvh_batch_step call (the
+ * first adds one: it computes the FP32 pack and CFL maxima from the FP64
+ * state; later steps get them from the previous step's corrector). */
 int32_t fvh_batch_launches_per_step(const fvh_batch *b);
 
 #ifdef __cplusplus

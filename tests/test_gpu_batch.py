@@ -151,3 +151,24 @@ def test_autotune_picks_a_shape_and_keeps_results(tmp_path, monkeypatch):
     assert np.all(codes == 0) and np.array_equal(t, tref)
     for k in range(len(meshes)):
         assert np.array_equal(b.get_state(k), ref[k])
+
+
+def test_steps_split_across_calls_bitwise():
+    """Within one fvh_batch_step call each corrector prepares the next step's
+    pack and per-problem CFL maxima; splitting the steps over several calls
+    (each starting from the FP64 state) must give the same bits."""
+    probs = _problems(6, seed=21)
+    tfs = [10.0, 0.01, 10.0, 0.02, 10.0, 10.0]
+    one, t1, c1, _ = _run_batch(probs, 24, tf=tfs)
+    p = _params()
+    meshes = [m for m, _ in probs]
+    b = H.Batch.for_meshes(p, meshes)
+    b.assign(meshes, 0.4, tfs)
+    for k, (m, kind) in enumerate(probs):
+        b.set_state(k, H.initial_state(kind, m, p, seed=k), 0.0)
+    for n in (5, 1, 7, 11):
+        b.step(n)
+    t2, c2, _ = b.query()
+    assert np.all(c1 == 0) and np.all(c2 == 0) and np.array_equal(t1, t2)
+    for k in range(len(meshes)):
+        assert np.array_equal(b.get_state(k), one[k])
