@@ -699,10 +699,11 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
 }
 
 // Neighbour records are loaded as the loop reaches them.  3D keeps
-// 7 x 3 gradient sums, 14 extrema and the 3x3 system live: up to 128
-// registers there, 64 in 2D.
+// 7 x 3 gradient sums, 14 extrema and the 3x3 system live: 96 registers
+// there (5 blocks of 128 per SM; measured faster than 128 registers with 4
+// blocks, or 80 with spills), 64 in 2D.
 template <int D, bool LIMIT, int BS>
-__global__ void __launch_bounds__(BS, (D == 2 ? 1024 : 512) / BS)
+__global__ void __launch_bounds__(BS, (D == 2 ? 1024 : 640) / BS)
 gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk, int rev) {
   for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_cells; i += gridDim.x * BS) {
     const int c0 = rev ? m.num_cells - 1 - i : i;
