@@ -197,20 +197,32 @@ class ClockSampler:
 # CPU baseline: the oracle (C++ restatement of the reference, OpenMP)
 # ---------------------------------------------------------------------------
 def cpu_baseline(mesh, params, state0, budget_s: float = 12.0, max_steps: int = 400) -> dict:
+    """The oracle (the reference's tasks restated in C++/OpenMP) on the host
+    cores: all threads (the reported value) and one thread."""
     import oracle
     from tests import _util as U
     O = oracle.load()
-    s = state0.copy()
-    U.oracle_run(O, mesh, s, params, 1)  # warm-up step
-    n, t0 = 0, time.perf_counter()
-    while n < max_steps and (time.perf_counter() - t0) < budget_s:
-        U.oracle_run(O, mesh, s, params, 1)
-        n += 1
-    dt = time.perf_counter() - t0
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+    def sample(budget):
+        s = state0.copy()
+        U.oracle_run(O, mesh, s, params, 1)  # warm-up step
+        n, t0 = 0, time.perf_counter()
+        while n < max_steps and (time.perf_counter() - t0) < budget:
+            U.oracle_run(O, mesh, s, params, 1)
+            n += 1
+        return n, time.perf_counter() - t0
+
+    O.oracle_set_threads(0)
+    cores = int(O.oracle_max_threads())
+    n, dt = sample(budget_s)
+    O.oracle_set_threads(1)
+    n1, dt1 = sample(budget_s / 3)
+    O.oracle_set_threads(0)
     return {"value": mesh.num_cells * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{n} full time steps of the {N_SIDE}x{N_SIDE} workload in {dt:.1f} s "
-                      f"(FP64, HLLC; oracle/hydro_oracle.cpp, -O2, OpenMP)"}
+                      f"(FP64, HLLC; oracle/hydro_oracle.cpp, -O2, OpenMP)",
+            "one_thread": {"value": mesh.num_cells * n1 / dt1, "cores": 1,
+                           "sample": f"{n1} steps in {dt1:.1f} s"}}
 
 
 # ---------------------------------------------------------------------------
@@ -251,7 +263,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     U.oracle_run(O, mesh, s, p64, args.steps)
     dt = time.perf_counter() - t0
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cores = int(O.oracle_max_threads())
     value = mesh.num_cells * args.steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
@@ -310,11 +322,32 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
     if np.any(codes != 0):
         raise RuntimeError(f"batched: device status {codes[codes != 0][:4]}")
     nc = b.num_cells
+    # accuracy: sampled problems (smallest, median, largest) rerun alone in FP64
+    # for the same number of steps
+    sizes = [m.num_cells for m in meshes]
+    order = np.argsort(sizes)
+    acc = []
+    p64 = H.make_params(2, flux="hllc", precision="fp64", boundary="outflow", swap=False,
+                        cfl=0.4, final_time=1.0e9)
+    E = lambda s: s[0] * (s[3] + 0.5 * (s[1] ** 2 + s[2] ** 2))
+    for k in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+        m, kind = probs[k]
+        dm, ds = H.DeviceMesh(m), H.DeviceState(2, m.num_cells)
+        sol = H.Solver(dm, p64)
+        ds.upload(H.initial_state(kind, m, p64, seed=k), stream)
+        sol.reset(0.0, stream)
+        sol.run(ds, warmup + steps, stream=stream)  # the autotuner restores the state
+        ref, mix = ds.download(stream), b.get_state(k, stream)
+        acc.append({"problem": k, "cells": m.num_cells, "kind": kind,
+                    "l1_density": float(np.abs(mix[0] - ref[0]).sum() / np.abs(ref[0]).sum()),
+                    "linf_density": float(np.abs(mix[0] - ref[0]).max()),
+                    "l1_total_energy": float(np.abs(E(mix) - E(ref)).sum() / np.abs(E(ref)).sum())})
     return {"value": nc * steps / (ms * 1e-3), "unit": UNIT, "problems": len(meshes),
             "cells": nc, "steps": steps, "ms_per_step": ms / steps,
             "launches": "one CUDA graph launch for all steps",
             "gpu_launches": b.launches_per_step() * steps + 1,  # + the first step's pack
             "autotuned_shape": tune, "host_setup_s": setup_s,
+            "accuracy_vs_fp64": acc,
             "config": "512 independent 2D problems, cells log-uniform in [32^2, 512^2] (seed 3), "
                       "KH shear layer / four-quadrant / Sod, HLLC, outflow, textbook reconstruction, CFL 0.4, "
                       "mixed precision"}

@@ -48,6 +48,10 @@ def load() -> C.CDLL:
         L.oracle_evaluate_fluxes.restype = None
         L.oracle_apply_update.argtypes = [mp, pp, C.c_double, C.c_double, fp, sp, dp, i64p]
         L.oracle_apply_update.restype = C.c_int
+        L.oracle_set_threads.argtypes = [C.c_int32]
+        L.oracle_set_threads.restype = None
+        L.oracle_max_threads.argtypes = []
+        L.oracle_max_threads.restype = C.c_int32
         L.oracle_run.argtypes = [mp, pp, sp, C.c_int64, C.c_int, dp, i64p, i64p]
         L.oracle_run.restype = C.c_int
         L.oracle_state_from_pressure.argtypes = [C.c_int32, C.c_double, C.c_double, dp, dp,

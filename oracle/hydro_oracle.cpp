@@ -33,6 +33,8 @@
 #include <cstring>
 #include <vector>
 
+#include <omp.h>
+
 #include "flecsale_gb300.h"
 
 namespace {
@@ -605,5 +607,9 @@ void oracle_face_flux(int32_t dim, int32_t kind, const double *wl,
     else hlle<3>(l, r, n, f);
   }
 }
+
+// OpenMP threads the oracle's loops use (the CPU baseline times 1 and all).
+void oracle_set_threads(int32_t n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+int32_t oracle_max_threads(void) { return omp_get_max_threads(); }
 
 }  // extern "C"
