@@ -708,6 +708,7 @@ fvh_status fvh_batch_autotune(fvh_batch *b, int32_t trial_steps, int32_t use_cac
     cudaEventCreate(&e1);
     for (const auto &c : cands) {
       if (e != cudaSuccess) break;
+      if (c.schedule == 2) continue;  // the batch has no face colouring
       b->shape = c;
       drop_graphs(b);
       copy_state(false);

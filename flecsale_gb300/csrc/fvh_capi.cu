@@ -364,7 +364,8 @@ static fvh_status solver_step_flags(fvh_solver *s, const fvh_state_view *state, 
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule) {
   if (!s || (block != 128 && block != 256) || cells_per_thread < 1 || cells_per_thread > 8 ||
-      (schedule != 0 && schedule != 1))
+      schedule < 0 || schedule > 2 ||
+      (schedule == 2 && fvh::mixed::colours(s->mixed) == 0))
     return FVH_ERR_INVALID_ARGUMENT;
   s->shape.block = block;
   s->shape.cells_per_thread = cells_per_thread;
@@ -484,16 +485,20 @@ int64_t fvh_solver_launches_per_run(const fvh_solver *s, int64_t nsteps) {
     return nsteps * fvh_solver_launches_per_step(s);
   int64_t total = 0;
   for (int64_t k = 0; k < nsteps && k < 2; ++k)  // the first step and one of the rest
-    total += fvh::mixed::launches_per_step(s->params, s->shape, chunk_flags(k, nsteps));
+    total += fvh::mixed::launches_per_step(s->params, s->shape, chunk_flags(k, nsteps),
+                                           fvh::mixed::colours(s->mixed));
   if (nsteps > 2)
-    total += (nsteps - 2) * fvh::mixed::launches_per_step(s->params, s->shape, chunk_flags(1, nsteps));
+    total += (nsteps - 2) * fvh::mixed::launches_per_step(s->params, s->shape,
+                                                          chunk_flags(1, nsteps),
+                                                          fvh::mixed::colours(s->mixed));
   return total;
 }
 
 int32_t fvh_solver_launches_per_step(const fvh_solver *s) {
   if (!s) return 0;
   if (s->params.precision == FVH_PRECISION_MIXED)
-    return fvh::mixed::launches_per_step(s->params, s->shape);
+    return fvh::mixed::launches_per_step(s->params, s->shape, {},
+                                         fvh::mixed::colours(s->mixed));
   // dt (partial + final) + per stage: gradients (or D*(D+4) memsets), fluxes, update
   const int D = s->mesh.dim;
   const int grad = s->params.order == 1 ? D * (D + 4) : 1;

@@ -29,6 +29,7 @@
 
 #include <cstdint>
 #include <new>
+#include <vector>
 
 #include "fvh_kernels.h"
 #include "fvh_mixed.h"
@@ -40,6 +41,8 @@ namespace mixed {
 using phys::prim;
 using phys::smax;
 using phys::smin;
+
+constexpr int kMaxColours = 32;
 
 // per-cell AoS record sizes in float4 units
 template <int D>
@@ -77,6 +80,12 @@ struct workspace {
   float *ell_vdx = nullptr;
   unsigned *ticket = nullptr;  // blocks done (the last one computes dt)
   unsigned *dtinv_max = nullptr;  // corrector's CFL maximum for the next step (FP32 bits)
+  // colour schedule (single mesh): faces grouped by colour, no two faces of a
+  // colour share a cell; per-cell compensated face sums (hi[D+2], lo[D+2])
+  int *colour_faces = nullptr;
+  float *acc = nullptr;
+  int ncolours = 0;
+  int colour_off[kMaxColours + 1] = {};
 };
 
 __device__ __forceinline__ void stg256(float4 *p, float4 a, float4 b) {
@@ -1133,6 +1142,71 @@ gather_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
   if (NEXT == 2) finish_cfl(w, nd, dt_inv);
 }
 
+// Colour schedule, part 1 (one launch per colour): one flux per face of the
+// colour, subtracted from / added to its cells' compensated sums.  No two
+// faces of a colour share a cell, so the read-modify-writes do not race; a
+// cell receives its faces in colour order (deterministic, but not the cell's
+// face order of the gather schedules, so the sums round differently).
+template <int D, int KIND, bool SECOND, int BS>
+__global__ void __launch_bounds__(BS, 1024 / BS)
+face_colour_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk_in,
+                   int swap, int outflow, int first, int count) {
+  constexpr int NQ = D + 2;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < count; i += gridDim.x * BS) {
+    const int f = w.colour_faces[first + i];
+    float F[NQ];
+    face_flux_area<D, KIND, SECOND>(m, w, pk_in, f, swap, outflow, F);
+    const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int c = side == 0 ? cc.x : cc.y;
+      if (c < 0) continue;
+      float *a = w.acc + (size_t)2 * NQ * c;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        float hi = a[k], lo = a[NQ + k];
+        two_sum_acc(hi, lo, side == 0 ? -F[k] : F[k]);
+        a[k] = hi;
+        a[NQ + k] = lo;
+      }
+    }
+  }
+}
+
+// Colour schedule, part 2: each cell takes its sums (and clears them for the
+// next stage), then the update of the gather schedules.
+template <int D, int BS, int STAGE, int NEXT = 0>
+__global__ void __launch_bounds__(BS, 1024 / BS)
+colour_update_kernel(const fvh_mesh_view m, const fvh_state_view s, workspace w,
+                     float4 *__restrict__ pk_out, const problem_map pm,
+                     const update_consts uc, int rev, const next_dt nd,
+                     const fvh_state_view out, int has_out) {
+  constexpr int NQ = D + 2;
+  stage_dt sdt;
+  float dt_inv = 0.f;
+  for (int i = blockIdx.x * BS + threadIdx.x; i < m.num_cells; i += gridDim.x * BS) {
+    const int c = rev ? m.num_cells - 1 - i : i;
+    const int pr = pm.cell_problem ? pm.cell_problem[c] : 0;
+    float *a = w.acc + (size_t)2 * NQ * c;
+    float shi[NQ], slo[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      shi[k] = a[k];
+      slo[k] = a[NQ + k];
+      a[k] = a[NQ + k] = 0.f;
+    }
+    if (!sdt.at(pm, c, pr, uc.factor)) {
+      if (NEXT == 2) dt_inv = smax(untouched_cfl<D>(m, w, c), dt_inv);
+      continue;
+    }
+    float vn[D], an;
+    cell_update<D, STAGE>(s, w, pk_out, pm, c, pr, sdt.dts, shi, slo, uc, vn, &an,
+                          STAGE == 1 && has_out ? &out : nullptr);
+    if (NEXT == 2) dt_inv = smax(cell_cfl<D>(m, w, c, vn, an), dt_inv);
+  }
+  if (NEXT == 2) finish_cfl(w, nd, dt_inv);
+}
+
 // Diagnostic: the integer-pipe conversions applied to an array, so they can be
 // compared with exact host conversions.
 __global__ void split_kernel(const double *x, int64_t n, float *hi, float *lo, float *h2,
@@ -1236,11 +1310,52 @@ fvh_status create_capacity(int dim, int64_t cells, int64_t faces, int64_t vertic
   return FVH_OK;
 }
 
+// Greedy face colouring on the host (faces in id order, the smallest colour
+// neither cell uses yet) for the colour schedule; deterministic.
+static cudaError_t setup_colours(workspace *w, const fvh_mesh_view &m) {
+  std::vector<int32_t> fc(2 * (size_t)m.num_faces);
+  cudaError_t e = cudaMemcpy(fc.data(), m.face_cells, sizeof(int32_t) * fc.size(),
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  std::vector<uint32_t> used(m.num_cells, 0u);
+  std::vector<int> colour(m.num_faces);
+  int nc = 0;
+  for (int f = 0; f < m.num_faces; ++f) {
+    const int a = fc[2 * (size_t)f], b = fc[2 * (size_t)f + 1];
+    const uint32_t taken = used[a] | (b >= 0 ? used[b] : 0u);
+    int col = 0;
+    while (col < kMaxColours && (taken >> col) & 1u) ++col;
+    if (col == kMaxColours) return cudaErrorNotSupported;  // more than 32 colours
+    colour[f] = col;
+    used[a] |= 1u << col;
+    if (b >= 0) used[b] |= 1u << col;
+    nc = col + 1 > nc ? col + 1 : nc;
+  }
+  std::vector<int> off(nc + 1, 0), faces(m.num_faces);
+  for (int f = 0; f < m.num_faces; ++f) off[colour[f] + 1]++;
+  for (int k = 0; k < nc; ++k) off[k + 1] += off[k];
+  std::vector<int> pos(off.begin(), off.end() - 1);
+  for (int f = 0; f < m.num_faces; ++f) faces[pos[colour[f]]++] = f;
+  w->ncolours = nc;
+  for (int k = 0; k <= nc; ++k) w->colour_off[k] = off[k];
+  const int NQ = w->dim + 2;
+  e = cudaMalloc(&w->colour_faces, sizeof(int) * (size_t)m.num_faces);
+  if (e == cudaSuccess) e = cudaMalloc(&w->acc, sizeof(float) * 2 * NQ * (size_t)m.num_cells);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(w->colour_faces, faces.data(), sizeof(int) * faces.size(),
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(w->acc, 0, sizeof(float) * 2 * NQ * (size_t)m.num_cells);
+  return e;
+}
+
+int colours(const workspace *w) { return w ? w->ncolours : 0; }
+
 fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) {
   (void)p;
   const fvh_status r = create_capacity(m.dim, m.num_cells, m.num_faces, m.num_vertices, out);
   if (r != FVH_OK) return r;
   cudaError_t e = setup_geometry(*out, m, nullptr);
+  if (e == cudaSuccess) e = setup_colours(*out, m);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     destroy(*out);
@@ -1252,6 +1367,8 @@ fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) 
 
 void destroy(workspace *w) {
   if (!w) return;
+  cudaFree(w->colour_faces);
+  cudaFree(w->acc);
   cudaFree(w->base);
   delete w;
 }
@@ -1290,7 +1407,26 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
   k.factor = 0.5f;
   k.inv_cv = 1.0 / p.cv;
   k.unit_cv = p.cv == 1.0;
-  if (schedule == 1) {
+  if (schedule == 2) {
+    for (int col = 0; col < w->ncolours; ++col) {
+      const int first = w->colour_off[col], count = w->colour_off[col + 1] - first;
+      const int nbc = (int)((count + per - 1) / per);
+      face_colour_kernel<D, KIND, SECOND, BS><<<nbc > 0 ? nbc : 1, BS, 0, st>>>(
+          m, *w, pk_in, p.recon_swap_ep, p.boundary, first, count);
+      mark("face_colour");
+    }
+    dir ^= 1;
+    if (stage == 0)
+      colour_update_kernel<D, BS, 0><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
+                                                        ndv.out, 0);
+    else if (next)
+      colour_update_kernel<D, BS, 1, 2><<<nb_next, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir,
+                                                                 ndv, ndv.out, ndv.has_out);
+    else
+      colour_update_kernel<D, BS, 1><<<nb, BS, 0, st>>>(m, s, *w, pk_out, pm, k, dir, ndv,
+                                                        ndv.out, ndv.has_out);
+    mark("colour_update");
+  } else if (schedule == 1) {
     const int nbf = (int)((m.num_faces + per - 1) / per);
     dir ^= 1;
     face_flux_kernel<D, KIND, SECOND, BS><<<nbf, BS, 0, st>>>(m, *w, pk_in, p.recon_swap_ep,
@@ -1437,8 +1573,10 @@ cudaError_t step_batch(workspace *w, const fvh_mesh_view &m, const fvh_params &p
                     : step_batch_d<3>(w, m, p, s, pm, shape, st, mark, f);
 }
 
-int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f) {
-  const int per_stage = (p.order == 1 ? 0 : 1) + (sh.schedule == 1 ? 2 : 1);
+int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f,
+                      int ncolours) {
+  const int fluxes = sh.schedule == 2 ? ncolours + 1 : sh.schedule == 1 ? 2 : 1;
+  const int per_stage = (p.order == 1 ? 0 : 1) + fluxes;
   return (f.pack_first ? 1 : 0) + 2 * per_stage;
 }
 

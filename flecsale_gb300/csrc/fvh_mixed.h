@@ -29,20 +29,26 @@ struct launch_mark {
   }
 };
 
-// Launch shape of the cell kernels (picked by the autotuner).  All shapes give
-// the same results bit for bit.
+// Launch shape of the cell kernels (picked by the autotuner).  Schedules 0
+// and 1 and every block size / cells per thread give the same results bit for
+// bit; schedule 2 sums each cell's face fluxes in another order.
 struct launch_shape {
   int block = 128;          // threads per block: 128 or 256
   int cells_per_thread = 1; // grid = ceil(cells / (block * cells_per_thread)), grid-stride
   int schedule = 0;         // 0: cell-centric (each cell evaluates its faces' fluxes);
-                            // 1: one flux per face into an array, then a cell gather
+                            // 1: one flux per face into an array, then a cell gather;
+                            // 2: face colouring (single mesh only): per colour, one
+                            //    flux per face added to its cells' sums, then the update
 };
 
-// Candidate shapes the autotuners time.
-constexpr int kNumShapes = 7;
+// Candidate shapes the autotuners time (the batch form skips schedule 2).
+constexpr int kNumShapes = 9;
 constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2, 0},
                                               {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
-                                              {128, 2, 1}};
+                                              {128, 2, 1}, {128, 1, 2}, {256, 1, 2}};
+
+// Number of face colours of a workspace made by create() (0 for the batch's).
+int colours(const workspace *w);
 
 // Steps of one run on a state nothing else writes in between: the corrector
 // of a step can also write the next step's FP32 pack and dt (the same bits
@@ -68,7 +74,8 @@ cudaError_t step(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
 
 // Kernel launches per step.
 int launches_per_step(const fvh_params &p);
-int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags());
+int launches_per_step(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags(),
+                      int ncolours = 0);
 int launches_per_step_batch(const fvh_params &p, const launch_shape &sh, step_flags f = step_flags());
 
 // Independent problems concatenated into one mesh: problem k owns the cells

@@ -281,10 +281,14 @@ const fvh_flux_view *fvh_solver_fluxes(fvh_solver *s);
 int32_t fvh_solver_launches_per_step(const fvh_solver *s);
 
 /* Launch shape of the mixed form's cell kernels: block 128 or 256, cells per
- * thread 1..8, schedule 0 (each cell evaluates its faces' fluxes) or 1 (one
- * flux per face into an array, then a cell gather).  Every shape gives the
- * same results bit for bit.  The FP64 form ignores it.  No reference
- * counterpart: the reference's tasks have no launch configuration. */
+ * thread 1..8, schedule 0 (each cell evaluates its faces' fluxes), 1 (one
+ * flux per face into an array, then a cell gather) or 2 (face colouring: for
+ * each colour of a greedy colouring in which no two faces of a colour share a
+ * cell, one flux per face added to its cells' compensated sums; then the
+ * update).  Schedules 0 and 1 and all block sizes / cells per thread give the
+ * same bits; schedule 2 adds each cell's fluxes in colour order, so its sums
+ * round differently (deterministically).  The FP64 form ignores it.  No
+ * reference counterpart: the reference's tasks have no launch configuration. */
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule);
 

@@ -254,3 +254,45 @@ def test_advance_host_pinned_equals_copies(cuda, nsteps):
         assert np.array_equal(h, res[0][0])
         assert np.array_equal(d, res[0][2])
     assert not np.array_equal(res[0][0], s0[:7])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_colour_schedule(cuda, dim):
+    """Schedule 2 (face colouring): deterministic, conservative, within
+    1e-10 relative L1 of the gather schedules (its sums add each cell's
+    fluxes in colour order), and a run equals single steps bitwise."""
+    torch = cuda
+    n = (90, 70) if dim == 2 else (14, 12, 10)
+    mesh = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, 0.2 if dim == 2 else 0.15, 8)
+    for bc in ("outflow", "wall"):
+        p = H.make_params(dim, flux="hllc", cfl=0.4 if dim == 2 else 0.3, precision="mixed",
+                          boundary=bc)
+        s0 = H.initial_state("four_quadrant" if dim == 2 else "inner_cube", mesh, p, seed=5)
+        dmesh = H.DeviceMesh(mesh)
+        stream = torch.cuda.Stream()
+        out = {}
+        for label, shape, mode in (("gather", (128, 1, 1), "run"), ("colour", (128, 1, 2), "run"),
+                                   ("colour2", (256, 1, 2), "run"),
+                                   ("colour_steps", (128, 1, 2), "steps")):
+            ds = H.DeviceState(dim, mesh.num_cells)
+            sol = H.Solver(dmesh, p)
+            sol.set_shape(*shape)
+            ds.upload(s0, stream)
+            sol.reset(0.0, stream)
+            if mode == "run":
+                sol.run(ds, 16, stream=stream)
+            else:
+                for _ in range(16):
+                    sol.step(ds, stream)
+            code, t, _ = sol.status(stream)
+            assert code == 0
+            out[label] = (ds.download(stream), t)
+        g, c = out["gather"][0], out["colour"][0]
+        assert np.abs(c[0] - g[0]).sum() / np.abs(g[0]).sum() <= 1e-10
+        assert np.array_equal(out["colour"][0], out["colour2"][0])
+        assert np.array_equal(out["colour"][0], out["colour_steps"][0])
+        if bc == "wall":
+            vol = mesh.arrays()["cell_volume"]
+            m0, e0 = _totals(s0, vol, dim)
+            m1, e1 = _totals(c, vol, dim)
+            assert abs(m1 - m0) / m0 < 1e-12 and abs(e1 - e0) / e0 < 1e-12
