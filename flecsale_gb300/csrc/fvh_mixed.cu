@@ -18,10 +18,13 @@
 //                updates (tasks.h:589-659)
 //   schedule 1:  face_flux (one flux per face into an array) + gather_update
 //                (the same sums in the same order, then the update)
+//   schedule 2:  face_colour per colour (fluxes added to both cells' sums) +
+//                colour_update
 //   predictor update: writes the double-float increments and the FP32 pack of
 //                the predicted state, no FP64 state
 //   (gradients, fluxes again for the corrector, whose update writes the FP64
-//   state = old state + both stages' increments)
+//   state = old state + both stages' increments; inside a run it also writes
+//   the next step's pack and dt, and that step skips pack_dt)
 //
 // A face flux has the same bits wherever it is evaluated, so the update is
 // conservative to double-float rounding without atomics.
