@@ -147,6 +147,15 @@ def ncu_traffic() -> dict:
         return {}
 
 
+def ncu_pipes() -> dict:
+    """Per-kernel pipe utilisation (fractions) from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "pipe_utilization.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -568,7 +577,11 @@ def run_ours(args):
                        "ms_per_step": results["fp64"]["ms"] / args.steps,
                        "gpu_launches": results["fp64"]["launches"],
                        "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "fp64"),
-                       "roofline": roofline("fp64")},
+                       "roofline": dict(roofline("fp64"), fp64_pipe_active=ncu_pipes().get(
+                           "fp64:gradients", {}).get("fp64"),
+                           note="FP64-pipe bound: GB300 issues 2 FP64 operations per clock "
+                                "per SM; fp64_pipe_active is the ncu figure of the dominant "
+                                "kernel (profiles/fp64_gradients_1024sq_four_quadrant.md)")},
         "mixed_over_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "accuracy": {"steps": args.warmup + args.steps,
                      "l1_density_mixed_vs_fp64": l1(m[0], f[0]),
