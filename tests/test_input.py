@@ -41,7 +41,7 @@ def test_shock_box_3d_input_with_mesh_table():
 
 @pytest.mark.parametrize("name", ["2d/shock_box_2d.lua", "3d/shock_box_3d.lua"])
 def test_reference_input_files(name):
-    path = os.path.join("/root/reference/apps/hydro", name)
+    path = os.path.join(U.REFERENCE, "apps/hydro", name)
     if not os.path.exists(path):
         pytest.skip("reference checkout not present")
     inp = H.Input(path)

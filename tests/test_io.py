@@ -35,7 +35,7 @@ def golden_2d_text():
 
 
 def test_golden_text_rebuild_matches_reference_file():
-    ref = "/root/reference/apps/hydro/2d/shock_box_2d-solution_rank000000.txt.1procs.std"
+    ref = os.path.join(U.REFERENCE, "apps/hydro/2d/shock_box_2d-solution_rank000000.txt.1procs.std")
     if not os.path.exists(ref):
         pytest.skip("reference checkout not present")
     exp = [l.rstrip() for l in open(ref).read().splitlines()]
@@ -120,7 +120,7 @@ def test_exodus_reader_quad_and_hex(tmp_path):
 
 
 def test_exodus_reader_on_reference_meshes():
-    root = "/root/reference/data/meshes"
+    root = os.path.join(U.REFERENCE, "data/meshes")
     if not os.path.isdir(root):
         pytest.skip("reference checkout not present")
     m = H.read_exodus(os.path.join(root, "sedov_20x20x20.g"))
