@@ -59,8 +59,9 @@ struct layout {
   static constexpr int FLUX4 = D == 2 ? 1 : 2; // face flux (D+2 floats, padded)
   static constexpr int DEL4 = D == 2 ? 2 : 3;  // predictor increments (D+2 double-floats)
   // ELL width of the vertex-offset table (vertices beyond come from the mesh
-  // CSR): what a quadrilateral / hexahedral cell has
-  static constexpr int W_CV = D == 2 ? 4 : 8;
+  // CSR and the vertex coordinates): a quadrilateral's 4 in 2D; none in 3D,
+  // where 8 offsets (96 B/cell) cost more than the CSR + coordinate gathers
+  static constexpr int W_CV = D == 2 ? 4 : 0;
 };
 
 struct workspace {
