@@ -358,7 +358,8 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
         acc.append({"problem": k, "cells": m.num_cells, "kind": kind,
                     "l1_density": float(np.abs(mix[0] - ref[0]).sum() / np.abs(ref[0]).sum()),
                     "linf_density": float(np.abs(mix[0] - ref[0]).max()),
-                    "l1_total_energy": float(np.abs(E(mix) - E(ref)).sum() / np.abs(E(ref)).sum())})
+                    "l1_total_energy": float(np.abs(E(mix) - E(ref)).sum() / np.abs(E(ref)).sum()),
+                    "linf_total_energy": float(np.abs(E(mix) - E(ref)).max())})
     return {"value": nc * steps / (ms * 1e-3), "unit": UNIT, "problems": len(meshes),
             "cells": nc, "steps": steps, "ms_per_step": ms / steps,
             "launches": "one CUDA graph launch for all steps",
@@ -586,7 +587,8 @@ def run_ours(args):
         "accuracy": {"steps": args.warmup + args.steps,
                      "l1_density_mixed_vs_fp64": l1(m[0], f[0]),
                      "l1_total_energy_mixed_vs_fp64": l1(E(m), E(f)),
-                     "linf_density_mixed_vs_fp64": float(np.abs(m[0] - f[0]).max())},
+                     "linf_density_mixed_vs_fp64": float(np.abs(m[0] - f[0]).max()),
+                     "linf_total_energy_mixed_vs_fp64": float(np.abs(E(m) - E(f)).max())},
     }
     if not args.no_batch:
         line["batched"] = run_batched(torch, stream, min(args.steps, 50), args.warmup)
