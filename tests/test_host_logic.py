@@ -1,0 +1,64 @@
+"""Host-side logic that needs no GPU: the serving request stream, the bench's
+algorithmic-byte model and its reporting helpers."""
+import numpy as np
+
+import flecsale_gb300.hydro as H
+from flecsale_gb300 import serve
+
+
+def test_poisson_requests_deterministic_and_in_range():
+    a = serve.poisson_requests(5.0, 30.0, seed=4)
+    b = serve.poisson_requests(5.0, 30.0, seed=4)
+    assert [(r.arrival, r.side, r.t_end, r.seed) for r in a] == \
+           [(r.arrival, r.side, r.t_end, r.seed) for r in b]
+    assert 100 < len(a) < 200                       # ~ rate * duration
+    arr = np.array([r.arrival for r in a])
+    assert np.all(np.diff(arr) > 0) and arr[-1] < 30.0
+    sides = np.array([r.side for r in a])
+    assert sides.min() >= 64 and sides.max() <= 2048
+    # log-uniform sides: the median side is near the geometric mean
+    assert 250 < np.median(sides) < 500
+    tend = np.array([r.t_end for r in a])
+    assert tend.min() >= 0.05 and tend.max() <= 0.3
+    assert {r.kind for r in a} == {"kelvin_helmholtz", "four_quadrant", "sod"}
+
+
+def test_server_params_scheme():
+    p = serve.server_params()
+    assert p.precision == H.PRECISION["mixed"] and p.flux_kind == H.FLUX["hllc"]
+    assert p.recon_swap_ep == 0 and p.boundary == 1 and p.cfl == 0.4
+
+
+def test_admission_by_capacity():
+    """_fits admits a request while the running set plus it stays within
+    every capacity (cells, faces, vertices, problems)."""
+    srv = serve.Server.__new__(serve.Server)
+    srv.caps = (1000, 2200, 1200, 3)
+    reqs = [serve.build_mesh(serve.Request(k, 0.0, s, "sod", 0.1)) for k, s in
+            enumerate((20, 20, 10, 5))]
+    assert srv._fits([], reqs[0])                       # 400 cells
+    assert srv._fits([reqs[0]], reqs[1])                # 800
+    assert not srv._fits(reqs[:2], reqs[0])             # 1200 cells > 1000
+    assert srv._fits(reqs[:2], reqs[2])                 # 900 cells, 3 problems
+    assert not srv._fits(reqs[:3], reqs[3])             # a 4th problem
+
+
+def test_algorithmic_bytes_model():
+    import bench
+    m = H.HostMesh.box(2, (64, 48), [0, 0], [1, 1], 0.2, 1)
+    b = bench.algorithmic_bytes(m, "mixed")
+    assert all(v > 0 for v in b.values())
+    # a run's step (no pack_dt) moves less than a single step
+    single = b["pack_dt"] + 2 * b["gradients"] + b["flux_update_predictor"] + b["flux_update_corrector"]
+    assert bench.per_zone_update_bytes(m, "mixed") * m.num_cells < single
+    b64 = bench.algorithmic_bytes(m, "fp64")
+    f = bench.per_zone_update_bytes(m, "fp64")
+    assert 1300 < f < 1700                              # the 2D figure derived for the reference dataflow
+    assert b64["gradients"] > b64["update"]
+    m3 = H.HostMesh.box(3, (8, 8, 8), [0, 0, 0], [1, 1, 1], 0.1, 1)
+    assert bench.per_zone_update_bytes(m3, "fp64") > f  # 3D moves more per zone-update
+
+
+def test_max_over_ranks_without_a_group():
+    import bench
+    assert bench.max_over_ranks(None, 3.5) == 3.5
