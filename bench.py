@@ -622,11 +622,19 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=12.0,
                     help="arrival window of the serving run (0 skips it)")
     ap.add_argument("--n", type=int, default=N_SIDE, help="mesh side (default 1024)")
+    ap.add_argument("--only-3d", type=int, default=0, metavar="N",
+                    help="run only the 3D shock box on an N^3 mesh for --steps steps and print "
+                         "its record (profiling of the 3D kernels)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_3d:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_3d(torch, torch.cuda.Stream(), args.only_3d, args.steps)), flush=True)
+        return 0
     return run_ours(args)
 
 
