@@ -79,7 +79,6 @@ def algorithmic_bytes(mesh, precision: str) -> dict:
     grad4 = 3 if D == 2 else 6
     fdx4 = 1 if D == 2 else 2      # face offsets; also the face-flux record size
     del4 = 2 if D == 2 else 3      # predictor increments (double-float)
-    w_cv = 4 if D == 2 else 8      # vertex-offset table width
     state_in = 8 * (D + 2) * nc    # FP64 d, v, e read by an update
     face_geo = 8 * nf + 16 * nf + 16 * fdx4 * nf  # face cells, normal+area, offsets
     recon_in = 32 * nc + 16 * grad4 * nc           # FP32 pack + gradients
@@ -88,8 +87,10 @@ def algorithmic_bytes(mesh, precision: str) -> dict:
     b = {
         # FP64 state in (d, v, e, p, a), FP32 pack out, inv_vol32, faces, face geometry
         "pack_dt": 8 * (D + 4) * nc + 32 * nc + 4 * nc + csr_cf + 16 * nf,
-        "gradients": 32 * nc + 16 * cen4 * nc + csr_nb + 4 * (nc + 1)
-                     + 4 * w_cv * D * nc + 16 * grad4 * nc,
+        # pack + centroid per cell, neighbour CSR, cell-vertex CSR + vertex
+        # coordinates (hi/lo) for the limiter, gradients out
+        "gradients": 32 * nc + 16 * cen4 * nc + csr_nb + csr_cv + 16 * cen4 * nv
+                     + 16 * grad4 * nc,
         # schedule 0: fluxes evaluated by each cell, then the update
         "flux_update_predictor": recon_in + csr_cf + face_geo + 8 * nc + state_in + pred_out,
         "flux_update_corrector": recon_in + csr_cf + face_geo + 8 * nc + state_in + corr_io,

@@ -58,10 +58,6 @@ struct layout {
   static constexpr int FDX4 = D == 2 ? 1 : 2;  // x_f - x_c0, x_f - x_c1
   static constexpr int FLUX4 = D == 2 ? 1 : 2; // face flux (D+2 floats, padded)
   static constexpr int DEL4 = D == 2 ? 2 : 3;  // predictor increments (D+2 double-floats)
-  // ELL width of the vertex-offset table (vertices beyond come from the mesh
-  // CSR and the vertex coordinates): a quadrilateral's 4 in 2D; none in 3D,
-  // where 8 offsets (96 B/cell) cost more than the CSR + coordinate gathers
-  static constexpr int W_CV = D == 2 ? 4 : 0;
 };
 
 struct workspace {
@@ -78,10 +74,6 @@ struct workspace {
   float4 *delta = nullptr;   // predictor increments of (d, v.., e) as double-floats
   float *inv_vol32 = nullptr;  // 1/V rounded to FP32 (CFL estimate; update, high part)
   float *inv_vol_lo = nullptr; // 1/V - inv_vol32, rounded to FP32 (update, low part)
-  // Column-major ELL table of the offsets x_v - x_c (FP32) of each cell's
-  // first W_CV vertices, [(k * D + i) * nc + c]: a warp's 32 consecutive cells
-  // read 32 consecutive words, with no dependent index load
-  float *ell_vdx = nullptr;
   unsigned *ticket = nullptr;  // blocks done (the last one computes dt)
   unsigned *dtinv_max = nullptr;  // corrector's CFL maximum for the next step (FP32 bits)
   // colour schedule (single mesh): faces grouped by colour, no two faces of a
@@ -347,32 +339,6 @@ __global__ void setup_faces(const fvh_mesh_view m, workspace w) {
     w.fgeo[f] = make_float4(n[0], n[1], n[D - 1], area);
     w.fdx[2 * (size_t)f] = make_float4(d0[0], d0[1], d0[D - 1], 0.f);
     w.fdx[2 * (size_t)f + 1] = make_float4(d1[0], d1[1], d1[D - 1], 0.f);
-  }
-}
-
-// ELL vertex-offset table, computed exactly as the limiter's fallback computes
-// the offsets from the hi/lo coordinate splits.
-template <int D>
-__global__ void setup_lists(const fvh_mesh_view m, workspace w) {
-  using L = layout<D>;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.num_cells) return;
-  float xh[3], xl[3];
-#pragma unroll
-  for (int i = 0; i < D; ++i) {
-    const float2 t = split(m.cell_centroid[i][c]);
-    xh[i] = t.x;
-    xl[i] = t.y;
-  }
-  const int q0 = m.cell_vertex_offsets[c], n = m.cell_vertex_offsets[c + 1] - q0;
-  for (int k = 0; k < n && k < L::W_CV; ++k) {
-    const int v = m.cell_vertices[q0 + k];
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-      const float2 t = split(m.vertex_coord[i][v]);
-      w.ell_vdx[((size_t)k * D + i) * w.nc + c] =
-          __fadd_rn(__fsub_rn(t.x, xh[i]), __fsub_rn(t.y, xl[i]));
-    }
   }
 }
 
@@ -674,15 +640,7 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
         dneg[k] = fminf(du, dneg[k]);
       }
     };
-    const int ne = nr < layout<D>::W_CV ? nr : layout<D>::W_CV;
-    const float *vd = w.ell_vdx + c0;
-    for (int r = 0; r < ne; ++r, vd += (size_t)D * w.nc) {  // ELL offsets
-      float dxv[3];
-#pragma unroll
-      for (int i = 0; i < D; ++i) dxv[i] = vd[(size_t)i * w.nc];
-      vertex(dxv);
-    }
-    for (int r = ne; r < nr; ++r) {  // beyond the ELL width: from the coordinates
+    for (int r = 0; r < nr; ++r) {
       float vh[3], vl[3], dxv[3];
       load_cen<D>(w.vcoord, m.cell_vertices[r0 + r], vh, vl);
 #pragma unroll
@@ -1242,7 +1200,6 @@ static size_t bytes_for(int nc, int nf, int nv) {
   return sizeof(float4) * ((size_t)nc * (2 * L::PACK4 + L::GRAD4 + L::CEN4) + (size_t)nv * L::CEN4 +
                            (size_t)nf * (L::FGEO4 + L::FDX4 + L::FLUX4) + (size_t)nc * L::DEL4) +
          2 * sizeof(float) * (size_t)nc +
-         sizeof(float) * (size_t)nc * L::W_CV * D +
          256 * 18;  // alignment of each carved array + counters
 }
 
@@ -1266,7 +1223,6 @@ static void carve(workspace *w) {
   w->delta = reinterpret_cast<float4 *>(take(sizeof(float4) * (size_t)w->nc * L::DEL4));
   w->inv_vol32 = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
   w->inv_vol_lo = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc));
-  w->ell_vdx = reinterpret_cast<float *>(take(sizeof(float) * (size_t)w->nc * L::W_CV * D));
   w->ticket = reinterpret_cast<unsigned *>(take(256));
   w->dtinv_max = reinterpret_cast<unsigned *>(take(256));
 }
@@ -1277,7 +1233,6 @@ static cudaError_t setup_d(const fvh_mesh_view &m, workspace *w, cudaStream_t st
   setup_cells<D><<<(m.num_cells + t - 1) / t, t, 0, st>>>(m, *w);
   setup_vertices<D><<<(m.num_vertices + t - 1) / t, t, 0, st>>>(m, *w);
   setup_faces<D><<<(m.num_faces + t - 1) / t, t, 0, st>>>(m, *w);
-  setup_lists<D><<<(m.num_cells + t - 1) / t, t, 0, st>>>(m, *w);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,6 @@
 """The GPU path on cell shapes other than the box generator's quads and hexes:
 triangles, a quad/triangle mix and tetrahedra (Exodus TRI3/QUAD4 polygons and
-TETRA4), with more vertex neighbours than the ELL tables hold.  FP64 runs are
+TETRA4), with more vertex neighbours than the box cells have.  FP64 runs are
 bitwise equal to the oracle; the mixed form is within the 1e-4 L1 bar."""
 import numpy as np
 import pytest
@@ -85,5 +85,5 @@ def test_fp64_bitwise_and_mixed_close(cuda, name):
     mix, t_mix = _run(mesh, H.make_params(dim, precision="mixed", **kw), s0, nsteps)
     assert abs(t_mix - t) <= 1e-4 * t
     assert np.abs(mix[0] - ref[0]).sum() / np.abs(ref[0]).sum() <= 1e-4
-    if dim == 3:  # tet vertex neighbourhoods are larger than the hex ELL width
+    if dim == 3:  # tet vertex neighbourhoods are larger than a hex's 26
         assert mesh.nnz_nbrs / mesh.num_cells > 26
