@@ -41,6 +41,9 @@ CASES = [
     (2, (100, 10), "sod", "hllc", "barth_jespersen", 1, 60),
     (3, (24, 20, 16), "inner_cube", "rusanov", "barth_jespersen", 2, 20),
     (3, (24, 20, 16), "inner_cube", "hllc", "barth_jespersen", 2, 20, "outflow"),
+    # unlimited gradients (the limiter-free kernels)
+    (2, (128, 96), "kelvin_helmholtz", "hlle", "none", 2, 20),
+    (3, (24, 20, 16), "kelvin_helmholtz", "hllc", "none", 2, 10),
 ]
 
 
