@@ -432,28 +432,39 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (const auto &c : fvh::mixed::kShapes) {
-    if (e != cudaSuccess) break;
-    fvh_solver_set_shape(s, c.block, c.cells_per_thread, c.schedule);
-    refresh();
-    // timed as fvh_solver_run launches steps
-    fvh_status r = FVH_OK;
-    for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
-      r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
-    refresh();
-    cudaEventRecord(e0, st);
-    for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
-      r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
-    cudaEventRecord(e1, st);
-    if (r == FVH_OK) e = cudaEventSynchronize(e1);
-    if (r != FVH_OK || e != cudaSuccess) continue;
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (best_ms < 0 || ms / trial_steps < best_ms) {
-      best_ms = ms / trial_steps;
-      best = c;
+  // every shape timed in each of kAutotuneRounds interleaved rounds; a shape's
+  // figure is its fastest round (robust to a one-off slow trial)
+  constexpr int NS = fvh::mixed::kNumShapes;
+  double shape_ms[NS];
+  for (int i = 0; i < NS; ++i) shape_ms[i] = -1;
+  for (int round = 0; round < fvh::mixed::kAutotuneRounds; ++round) {
+    for (int i = 0; i < NS; ++i) {
+      const auto &c = fvh::mixed::kShapes[i];
+      if (e != cudaSuccess) break;
+      fvh_solver_set_shape(s, c.block, c.cells_per_thread, c.schedule);
+      refresh();
+      // timed as fvh_solver_run launches steps
+      fvh_status r = FVH_OK;
+      for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
+        r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
+      refresh();
+      cudaEventRecord(e0, st);
+      for (int k = 0; k < trial_steps && r == FVH_OK; ++k)
+        r = solver_step_flags(s, &tmp, st, chunk_flags(k, trial_steps));
+      cudaEventRecord(e1, st);
+      if (r == FVH_OK) e = cudaEventSynchronize(e1);
+      if (r != FVH_OK || e != cudaSuccess) continue;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double per = ms / trial_steps;
+      if (shape_ms[i] < 0 || per < shape_ms[i]) shape_ms[i] = per;
     }
   }
+  for (int i = 0; i < NS; ++i)
+    if (shape_ms[i] >= 0 && (best_ms < 0 || shape_ms[i] < best_ms)) {
+      best_ms = shape_ms[i];
+      best = fvh::mixed::kShapes[i];
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e == cudaSuccess)

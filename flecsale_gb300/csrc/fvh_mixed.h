@@ -46,6 +46,9 @@ constexpr int kNumShapes = 9;
 constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2, 0},
                                               {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
                                               {128, 2, 1}, {128, 1, 2}, {256, 1, 2}};
+// Interleaved timing rounds per shape in the autotuners (each shape keeps its
+// fastest round).
+constexpr int kAutotuneRounds = 2;
 
 // Number of face colours of a workspace made by create() (0 for the batch's).
 int colours(const workspace *w);
