@@ -11,7 +11,8 @@
 //                (a+|v.n|) A/V per block, the last block finishes dt
 //                (tasks.h:331-376)
 //   gradients    FP32 vertex-neighbour least squares + Barth-Jespersen limiter
-//                (tasks.h:145-321), FP32 AoS gradients
+//                (tasks.h:145-321), FP32 AoS gradients; in 2D on packed FP32
+//                pairs (FFMA2/FADD2/FMUL2)
 //   schedule 0:  flux_update: each cell reconstructs both sides of each of its
 //                faces, evaluates the Riemann/wall flux in FP32
 //                (tasks.h:385-464) and sums -/+F in its face order, then
