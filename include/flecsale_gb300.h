@@ -300,9 +300,10 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
                            double *hi_as_double, fvh_stream_t stream);
 
 /* Times each candidate launch shape for trial_steps steps on a scratch copy
- * of `state` and keeps the fastest; the state, solution time and status word
- * are left unchanged.  Synchronises; allocates the scratch copy.  No
- * reference counterpart. */
+ * of `state`, in two interleaved rounds (a shape's figure is its faster
+ * round), and keeps the fastest; the state, solution time and status word are
+ * left unchanged.  Synchronises; allocates the scratch copy.  No reference
+ * counterpart. */
 fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32_t trial_steps,
                                int32_t *block, int32_t *cells_per_thread, int32_t *schedule,
                                double *best_ms_per_step, fvh_stream_t stream);
