@@ -223,22 +223,28 @@ def test_run_equals_single_steps_bitwise(cuda, dim, schedule, final_time):
         assert out[0][1] == final_time
 
 
-@pytest.mark.parametrize("nsteps", [1, 4])
-def test_advance_host_pinned_equals_copies(cuda, nsteps):
+@pytest.mark.parametrize("dim,n,schedule,nsteps", [
+    (2, (120, 100), 0, 1), (2, (120, 100), 0, 4),
+    (2, (320, 256), 1, 1), (2, (320, 256), 1, 3), (3, (44, 40, 38), 1, 2)])
+def test_advance_host_pinned_equals_copies(cuda, dim, n, schedule, nsteps):
     """fvh_solver_advance_host with pinned host planes (kernels read and write
     host memory directly) gives the same bits as with pageable planes (copies)
     and as upload + run + download; the device state ends up the same too."""
     torch = cuda
-    mesh = H.HostMesh.box(2, (120, 100), [0, 0], [1, 1], 0.2, 9)
-    p = H.make_params(2, flux="hllc", cfl=0.4, precision="mixed", boundary="outflow")
-    s0 = H.initial_state("four_quadrant", mesh, p, seed=1)
+    mesh = H.HostMesh.box(dim, n, [0] * dim, [1] * dim, 0.2 if dim == 2 else 0.15, 9)
+    prob = "four_quadrant" if dim == 2 else "inner_cube"
+    p = H.make_params(dim, flux="hllc", cfl=0.4 if dim == 2 else 0.3, precision="mixed",
+                      boundary="outflow")
+    s0 = H.initial_state(prob, mesh, p, seed=1)
     dmesh = H.DeviceMesh(mesh)
     stream = torch.cuda.Stream()
     nc = mesh.num_cells
+    np_ = 5 + dim
     res = []
     for kind in ("pinned", "pageable", "run"):
-        ds = H.DeviceState(2, nc)
+        ds = H.DeviceState(dim, nc)
         sol = H.Solver(dmesh, p)
+        sol.set_shape(128, 1, schedule)
         if kind == "run":
             ds.upload(s0, stream)
             sol.reset(0.125, stream)
@@ -246,17 +252,17 @@ def test_advance_host_pinned_equals_copies(cuda, nsteps):
             host, t = ds.download(stream), sol.soln_time(stream)
         else:
             if kind == "pinned":
-                host = torch.empty((7, nc), dtype=torch.float64, pin_memory=True).numpy()
+                host = torch.empty((np_, nc), dtype=torch.float64, pin_memory=True).numpy()
             else:
-                host = np.empty((7, nc), np.float64)
-            host[:] = s0[:7]
+                host = np.empty((np_, nc), np.float64)
+            host[:] = s0[:np_]
             t = sol.advance_host(ds, host, nsteps, 0.125, stream)
         res.append((host.copy(), t, ds.download(stream)))
     for h, t, d in res[1:]:
         assert t == res[0][1]
         assert np.array_equal(h, res[0][0])
         assert np.array_equal(d, res[0][2])
-    assert not np.array_equal(res[0][0], s0[:7])
+    assert not np.array_equal(res[0][0], s0[:np_])
 
 
 @pytest.mark.parametrize("dim", [2, 3])
