@@ -680,8 +680,8 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // The same arithmetic with packed pairs (2D).  The values stay in the pack's
-// slot order (2D d vx vy p e a; 3D d vx vy vz
-// p e a) so that adjacent slots form the FP32 pairs of one packed instruction:
+// slot order (2D d vx vy p e a; 3D d vx vy vz p e a) so that adjacent slots
+// form the FP32 pairs of one packed instruction:
 // the differences, the least-squares sums, the solve, the vertex differences
 // and the limiting take 3 pair instructions per dimension (plus one scalar in
 // 3D) instead of 6 or 7 scalar ones.  u0 / the neighbours' records come as the
