@@ -42,6 +42,24 @@ def golden_3d():
     return mesh, z
 
 
+def two_rank_dumps():
+    """Per-rank dumps of apps/hydro/2d run on two ranks (544 cells each,
+    owned and ghost), from shock_box_2d_32x32_2procs.npz."""
+    return np.load(os.path.join(GOLDEN, "shock_box_2d_32x32_2procs.npz"))
+
+
+def two_rank_max_diff(cols: np.ndarray, centroids: np.ndarray, z2) -> float:
+    """Largest |difference| between single-domain dump columns (cells in the
+    order of `centroids`) and every cell listed in the two rank dumps, cells
+    matched by centroid (the ranks number their cells differently)."""
+    key = {(round(float(x), 9), round(float(y), 9)): i for i, (x, y) in enumerate(centroids)}
+    worst = 0.0
+    for r in (0, 1):
+        for (x, y), row in zip(z2[f"rank{r}_centroid"], z2[f"rank{r}_cells"]):
+            worst = max(worst, float(np.abs(cols[key[(round(float(x), 9), round(float(y), 9))]] - row).max()))
+    return worst
+
+
 def dump_columns(state: np.ndarray, dim: int) -> np.ndarray:
     """Cell columns of the reference dump: density internal_energy pressure velocity..."""
     return np.stack([state[0], state[1 + dim], state[2 + dim], *[state[1 + d] for d in range(dim)]], 1)

@@ -14,6 +14,10 @@ Outputs
   ref_physics_vectors.npz  outputs of the reference's own euler_eqns.h /
       flux.h / ideal_gas.h (compiled by oracle/ref_build.py) on seeded random
       states: wall, HLLE and Rusanov fluxes and the per-cell update.
+  shock_box_2d_32x32_2procs.npz  from apps/hydro/2d/shock_box_2d-solution_rank00000{0,1}.txt.2procs.std
+      (the same problem run on two ranks): per rank the 544 listed cells
+      (owned and ghost) as rank{r}_centroid (544,2), rank{r}_cells (544,5)
+      in the column order above, rank{r}_global_id; soln_time, iterations.
   shock_box_3d_20x20x20.npz  from apps/hydro/3d/shock_box_3d-solution_rank000000.txt.1procs.std
       and data/meshes/sedov_20x20x20.g (CDF-2, HEX8): exodus_coord (9261,3),
       exodus_connect (8000,8) zero-based, std_cell_centroid (8000,3),
@@ -60,6 +64,17 @@ def main(ref: str) -> None:
         os.path.join(here, "shock_box_2d_32x32.npz"),
         vertex_coord=v2[:, 2:4], cell_centroid=c2[:, 2:4], cells=c2[:, 4:9],
         soln_time=h2["soln_time"], iterations=h2["iterations"])
+
+    two = {}
+    for r in (0, 1):
+        hr, cr, _ = read_dump(os.path.join(
+            ref, f"apps/hydro/2d/shock_box_2d-solution_rank00000{r}.txt.2procs.std"))
+        assert hr["iterations"] == h2["iterations"] and hr["soln_time"] == h2["soln_time"]
+        two[f"rank{r}_centroid"] = cr[:, 2:4]
+        two[f"rank{r}_cells"] = cr[:, 4:9]
+        two[f"rank{r}_global_id"] = cr[:, 1].astype(np.int32)
+    np.savez_compressed(os.path.join(here, "shock_box_2d_32x32_2procs.npz"),
+                        soln_time=h2["soln_time"], iterations=h2["iterations"], **two)
 
     h3, c3, v3 = read_dump(os.path.join(
         ref, "apps/hydro/3d/shock_box_3d-solution_rank000000.txt.1procs.std"))

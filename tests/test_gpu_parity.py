@@ -139,6 +139,8 @@ def test_gpu_golden_2d(cuda):
     code, t, _ = solver.status()
     assert code == 0 and abs(t - float(z["soln_time"])) <= 1e-14
     assert U.numdiff_ok(z["cells"], U.dump_columns(out, 2), 1e-14)
+    # the reference's two-rank run of the same problem, cell by cell
+    assert U.two_rank_max_diff(U.dump_columns(out, 2), z["cell_centroid"], U.two_rank_dumps()) <= 1e-14
     O = __import__("oracle").load()
     U.oracle_run(O, mesh, state, p, 20)
     assert np.array_equal(out, state)

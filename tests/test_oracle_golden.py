@@ -28,6 +28,27 @@ def test_golden_2d_shock_box(fvh, oracle_lib):
     assert z["cells"][:, 0].min() < 0.11 and z["cells"][:, 0].max() > 1.0
 
 
+def test_golden_2d_two_rank_dumps(fvh, oracle_lib):
+    """The same problem run by the reference on two ranks lists 544 cells per
+    rank (owned and ghost); every one matches the single-domain oracle run
+    within the reference's regression tolerance (numdiff abs 1e-14; measured
+    8.4e-15, while the reference's own 1-rank and 2-rank dumps differ by up
+    to 1.02e-14)."""
+    mesh, z = U.golden_2d()
+    z2 = U.two_rank_dumps()
+    assert int(z2["iterations"]) == int(z["iterations"])
+    assert float(z2["soln_time"]) == float(z["soln_time"])
+    assert len(z2["rank0_cells"]) == len(z2["rank1_cells"]) == 544
+    # the two ranks together list every cell
+    ids = set(z2["rank0_global_id"].tolist()) | set(z2["rank1_global_id"].tolist())
+    assert len(ids) == mesh.num_cells
+    p = fvh.make_params(2)
+    state = fvh.initial_state("shock_box", mesh, p)
+    st, _, _ = U.oracle_run(oracle_lib, mesh, state, p, int(z["iterations"]))
+    assert st == 0
+    assert U.two_rank_max_diff(U.dump_columns(state, 2), z["cell_centroid"], z2) <= 1e-14
+
+
 def test_golden_2d_needs_the_reference_quirks(fvh, oracle_lib):
     """Without the e/p gradient swap (tasks.h:429-430) or with Rusanov instead of
     HLLE (types.h:118-125) the golden is not reproduced."""
