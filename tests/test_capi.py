@@ -60,3 +60,19 @@ def test_argument_errors_without_gpu(fvh):
     h = C.c_void_p()
     assert L.fvh_host_mesh_box(4, None, None, None, 0.0, 0, C.byref(h)) == H.ERR_INVALID_ARGUMENT
     assert L.fvh_time_step_workspace_bytes(10**6) == 8 * 1216
+
+
+def test_solver_and_batch_entry_points_reject_null_handles(fvh):
+    """The solver/batch entry points beyond the reference's tasks check their
+    handles and counts before any device call (no GPU needed)."""
+    L = fvh.lib()
+    EI = H.ERR_INVALID_ARGUMENT
+    sv = fvh.StateView()
+    i32, dbl = C.c_int32(), C.c_double()
+    assert L.fvh_solver_set_shape(None, 128, 1, 1) == EI
+    assert L.fvh_solver_autotune(None, C.byref(sv), 3, C.byref(i32), C.byref(i32),
+                                 C.byref(i32), C.byref(dbl), None) == EI
+    assert L.fvh_solver_advance_host(None, C.byref(sv), None, 1, C.byref(dbl), None) == EI
+    assert L.fvh_solver_launches_per_run(None, 10) == 0
+    assert L.fvh_debug_split(None, -1, None, None, None, None, None) == EI
+    assert L.fvh_batch_step(None, 1, None) == EI
