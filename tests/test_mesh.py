@@ -92,3 +92,21 @@ def test_tet_mesh(fvh):
     assert m.num_faces == 7
     assert np.sum(a["face_cells"][:, 1] >= 0) == 1
     np.testing.assert_allclose(a["cell_volume"][0], 1 / 6, rtol=1e-14)
+
+
+def test_box_beyond_int32_connectivity_is_refused(fvh):
+    """Meshes whose int32 CSR would overflow are refused before any
+    allocation: 2D 23171^2 cells need 4 * 5.4e8 > 2^31 cell-vertex entries;
+    3D 820^3 cells need 8 * 5.5e8."""
+    for dim, n in ((2, (23171, 23171)), (3, (820, 820, 820))):
+        with pytest.raises(H.FvhError) as e:
+            H.HostMesh.box(dim, n, [0] * dim, [1] * dim)
+        assert e.value.code == H.ERR_CAPACITY
+
+
+def test_box_rejects_empty_and_inverted_extents(fvh):
+    for n, lo, hi in (((0, 4), [0, 0], [1, 1]), ((4, 4), [0, 0], [1, 0]),
+                      ((4, -1), [0, 0], [1, 1])):
+        with pytest.raises(H.FvhError) as e:
+            H.HostMesh.box(2, n, lo, hi)
+        assert e.value.code == H.ERR_INVALID_ARGUMENT
