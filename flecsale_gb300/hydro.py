@@ -207,13 +207,32 @@ def check(code: int, what: str = "") -> None:
 
 
 def _dptr(a: np.ndarray):
-    assert a.dtype == np.float64 and a.flags.c_contiguous
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError(f"expected a C-contiguous float64 array, got {a.dtype} "
+                        f"(contiguous={a.flags.c_contiguous})")
     return a.ctypes.data_as(_dp)
 
 
 def _iptr(a: np.ndarray):
-    assert a.dtype == np.int32 and a.flags.c_contiguous
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        raise TypeError(f"expected a C-contiguous int32 array, got {a.dtype} "
+                        f"(contiguous={a.flags.c_contiguous})")
     return a.ctypes.data_as(_ip)
+
+
+def _state_planes(planes: np.ndarray, dim: int, num_cells: int, what: str,
+                  writable: bool = False) -> np.ndarray:
+    """The (5+dim, num_cells) FP64 planes d, v..., e, p, T, a the C ABI reads
+    (and, for writable, writes) in full; anything smaller would be read or
+    written past its end, so the shape is checked before the call."""
+    if planes.shape != (5 + dim, num_cells):
+        raise ValueError(f"{what}: state planes of shape {(5 + dim, num_cells)} expected, "
+                         f"got {planes.shape}")
+    if writable:
+        if planes.dtype != np.float64 or not planes.flags.c_contiguous or not planes.flags.writeable:
+            raise TypeError(f"{what}: a writable C-contiguous float64 array is required")
+        return planes
+    return np.ascontiguousarray(planes, np.float64)
 
 
 def stream_handle(stream) -> C.c_void_p:
@@ -392,7 +411,7 @@ class DeviceState:
         self.dim, self.num_cells = dim, num_cells
 
     def upload(self, planes: np.ndarray, stream=None) -> None:
-        planes = np.ascontiguousarray(planes, np.float64)
+        planes = _state_planes(np.asarray(planes), self.dim, self.num_cells, "upload")
         check(lib().fvh_state_upload(C.byref(self.view), self.dim, self.num_cells,
                                      _dptr(planes), stream_handle(stream)), "fvh_state_upload")
 
@@ -444,6 +463,7 @@ class Solver:
 
     def advance_host(self, state: DeviceState, planes: np.ndarray, nsteps: int, t: float,
                      stream=None) -> float:
+        _state_planes(planes, state.dim, state.num_cells, "advance_host", writable=True)
         tt = C.c_double(t)
         check(lib().fvh_solver_advance_host(self._h, C.byref(state.view), _dptr(planes),
                                             nsteps, C.byref(tt), stream_handle(stream)),
@@ -540,7 +560,10 @@ class Batch:
         self.meshes = list(meshes)
 
     def set_state(self, k: int, planes: np.ndarray, t: float = 0.0, stream=None) -> None:
-        planes = np.ascontiguousarray(planes[:5 + self.dim], np.float64)
+        if not 0 <= k < len(self.meshes):
+            raise IndexError(f"set_state: problem {k} of {len(self.meshes)}")
+        planes = _state_planes(np.asarray(planes)[:5 + self.dim], self.dim,
+                               self.meshes[k].num_cells, "set_state")
         check(lib().fvh_batch_set_state(self._h, k, _dptr(planes), t, stream_handle(stream)),
               "fvh_batch_set_state")
 
@@ -558,7 +581,8 @@ class Batch:
         t = np.zeros(n)
         codes = (C.c_int32 * n)()
         bad = (C.c_int64 * n)()
-        lib().fvh_batch_query(self._h, _dptr(t), codes, bad, stream_handle(stream))
+        check(lib().fvh_batch_query(self._h, _dptr(t), codes, bad, stream_handle(stream)),
+              "fvh_batch_query")
         return t, np.array(codes[:], np.int32), np.array(bad[:], np.int64)
 
     def set_shape(self, block: int, cells_per_thread: int, schedule: int = 0) -> None:
@@ -612,7 +636,8 @@ def write_dump(path: str, mesh: HostMesh, planes: np.ndarray, soln_time: float,
                iterations: int) -> None:
     """Regression dump in the reference's format (apps/hydro/tasks.h:771-849)."""
     _declare_io(lib())
-    planes = np.ascontiguousarray(planes[:5 + mesh.dim], np.float64)
+    planes = _state_planes(np.asarray(planes)[:5 + mesh.dim], mesh.dim, mesh.num_cells,
+                           "write_dump")
     check(lib().fvh_dump_write(path.encode(), mesh._h, _dptr(planes), soln_time, iterations),
           "fvh_dump_write")
 

@@ -85,3 +85,40 @@ def test_reference_arm_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"]["cells"] == 48 * 48
+
+
+def test_binding_checks_plane_shapes_before_the_call():
+    """The C ABI reads (and advance_host writes) all (5+dim) x num_cells
+    doubles of a host state: the binding refuses smaller, larger, strided,
+    read-only or mistyped arrays before anything reaches the library."""
+    import pytest
+    good = np.zeros((7, 10))
+    assert H._state_planes(good, 2, 10, "t") is not None
+    assert H._state_planes(good, 2, 10, "t", writable=True) is good
+    for bad in (np.zeros((7, 9)), np.zeros((6, 10)), np.zeros((8, 10)), np.zeros(70)):
+        with pytest.raises(ValueError):
+            H._state_planes(bad, 2, 10, "t")
+    with pytest.raises(TypeError):
+        H._state_planes(np.zeros((7, 20))[:, ::2], 2, 10, "t", writable=True)
+    with pytest.raises(TypeError):
+        H._state_planes(np.zeros((7, 10), np.float32), 2, 10, "t", writable=True)
+    ro = np.zeros((7, 10))
+    ro.flags.writeable = False
+    with pytest.raises(TypeError):
+        H._state_planes(ro, 2, 10, "t", writable=True)
+    # read-only use converts a float32 array instead of refusing it
+    assert H._state_planes(np.zeros((8, 4), np.float32), 3, 4, "t").dtype == np.float64
+    with pytest.raises(TypeError):
+        H._dptr(np.zeros(4, np.float32))
+    with pytest.raises(TypeError):
+        H._iptr(np.zeros(4, np.int64))
+    with pytest.raises(TypeError):
+        H._dptr(np.zeros((4, 4))[:, 1])
+
+
+def test_write_dump_refuses_short_planes(tmp_path):
+    import pytest
+    mesh = H.HostMesh.box(2, (4, 3), [0, 0], [1, 1])
+    with pytest.raises(ValueError):
+        H.write_dump(str(tmp_path / "d.txt"), mesh, np.zeros((7, mesh.num_cells - 1)), 0.0, 0)
+    assert not (tmp_path / "d.txt").exists()
