@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -32,6 +33,8 @@ struct nc_var {
 };
 
 struct nc_file {
+  // netCDF's own limit on the dimensions of one variable (NC_MAX_VAR_DIMS)
+  static constexpr uint32_t kMaxVarDims = 1024;
   std::vector<uint8_t> buf;
   size_t pos = 0;
   bool cdf2 = false, bad = false;
@@ -104,7 +107,13 @@ struct nc_file {
         nc_var v;
         v.name = name();
         const uint32_t nd = u32();
-        for (uint32_t k = 0; k < nd; ++k) v.dims.push_back((int)u32());
+        // every dimension id must name a dimension of this file
+        if (nd > kMaxVarDims) { bad = true; break; }
+        for (uint32_t k = 0; k < nd && !bad; ++k) {
+          const uint32_t id = u32();
+          if (id >= dims.size()) bad = true;
+          v.dims.push_back((int)id);
+        }
         attrs(&v.text_attrs);
         v.type = (int)u32();
         v.vsize = u32();
@@ -119,9 +128,14 @@ struct nc_file {
       if (v.name == n) return &v;
     return nullptr;
   }
+  // elements of a variable; UINT64_MAX when the product overflows
   uint64_t count(const nc_var &v) const {
     uint64_t c = 1;
-    for (int d : v.dims) c *= dims[d].second;
+    for (int d : v.dims) {
+      const uint64_t n = dims[d].second;
+      if (n != 0 && c > UINT64_MAX / n) return UINT64_MAX;
+      c *= n;
+    }
     return c;
   }
   bool is_record(const nc_var &v) const { return !v.dims.empty() && dims[v.dims[0]].second == 0; }
@@ -130,7 +144,7 @@ struct nc_file {
     if (is_record(v)) return false;
     const uint64_t n = count(v);
     const int ts = type_size(v.type);
-    if (ts == 0 || v.begin + n * ts > buf.size()) return false;
+    if (ts == 0 || v.begin > buf.size() || n > (buf.size() - v.begin) / ts) return false;
     out->resize(n);
     const uint8_t *p = buf.data() + v.begin;
     for (uint64_t i = 0; i < n; ++i, p += ts) {
@@ -193,10 +207,16 @@ fvh_status fvh_host_mesh_read_exodus(const char *path, fvh_host_mesh **out) {
     std::vector<double> all;
     if (!v || v->dims.size() != 2 || !nc.read_f64(*v, &all)) return FVH_ERR_UNSUPPORTED;
     ncoord = (int)nc.dims[v->dims[0]].second;
+    if (ncoord < 2 || ncoord > 3) return FVH_ERR_UNSUPPORTED;
     const size_t nn = nc.dims[v->dims[1]].second;
-    for (int d = 0; d < ncoord && d < 3; ++d) xyz[d].assign(all.begin() + d * nn, all.begin() + (d + 1) * nn);
+    for (int d = 0; d < ncoord; ++d) xyz[d].assign(all.begin() + d * nn, all.begin() + (d + 1) * nn);
   }
+  // two or three coordinate arrays, all of one length that int32 ids can index
+  if (ncoord < 2) return FVH_ERR_UNSUPPORTED;
   const size_t nv = xyz[0].size();
+  if (nv == 0 || nv >= (size_t)INT32_MAX) return FVH_ERR_UNSUPPORTED;
+  for (int d = 1; d < ncoord; ++d)
+    if (xyz[d].size() != nv) return FVH_ERR_UNSUPPORTED;
   // element blocks connect1, connect2, ...
   std::vector<int32_t> off{0}, cells;
   int shape = 0;  // nodes per element of the first block
@@ -207,12 +227,21 @@ fvh_status fvh_host_mesh_read_exodus(const char *path, fvh_host_mesh **out) {
     std::vector<double> c;
     if (v->dims.size() != 2 || !nc.read_f64(*v, &c)) return FVH_ERR_UNSUPPORTED;
     const std::string et = attr(*v, "elem_type");
-    const int npe = (int)nc.dims[v->dims[1]].second;
+    const uint64_t npe64 = nc.dims[v->dims[1]].second;
+    if (npe64 < 3 || npe64 > 8) return FVH_ERR_UNSUPPORTED;
+    const int npe = (int)npe64;
     if (shape == 0) shape = npe;
     if (npe != shape) return FVH_ERR_UNSUPPORTED;  // mixed element shapes
     if (et.rfind("SHELL", 0) == 0) shell = true;
-    for (size_t k = 0; k < c.size(); k += npe) {
-      for (int q = 0; q < npe; ++q) cells.push_back((int32_t)c[k + q] - 1);
+    if (cells.size() + c.size() >= (size_t)INT32_MAX) return FVH_ERR_CAPACITY;
+    for (size_t k = 0; k + npe <= c.size(); k += npe) {
+      for (int q = 0; q < npe; ++q) {
+        // Exodus node ids are 1-based; anything else is a malformed file
+        const double id = c[k + q];
+        if (!(id >= 1 && id <= (double)nv) || id != std::floor(id))
+          return FVH_ERR_INVALID_ARGUMENT;
+        cells.push_back((int32_t)id - 1);
+      }
       off.push_back((int32_t)cells.size());
     }
   }

@@ -139,3 +139,39 @@ def test_state_from_dvp_matches_initial_state():
     s = H.initial_state("four_quadrant", mesh, p)
     out = H.state_from_dvp(2, s[0], s[1:3], s[4])
     assert np.array_equal(out, s[:7])
+
+
+def _connectivity_file(tmp_path, connect, coords=None):
+    box = H.HostMesh.box(2, (3, 2), [0, 0], [1, 1], 0.1, 3)
+    a = box.arrays()
+    p = str(tmp_path / "m.g")
+    _write_exodus(p, a["vertex_coord"].T.copy() if coords is None else coords,
+                  connect if connect is not None else a["cell_vertices"].reshape(-1, 4), "QUAD4")
+    return p, a
+
+
+def test_exodus_reader_refuses_bad_node_ids(tmp_path):
+    """Node ids outside 1..num_nodes are refused before they index anything."""
+    p, a = _connectivity_file(tmp_path, None)
+    assert H.read_exodus(p).num_cells == 6
+    cv = a["cell_vertices"].reshape(-1, 4)
+    for bad in (-1, a["vertex_coord"].shape[1], 1 << 20):  # 0-based: 0, nv + 1, far out
+        c = cv.copy()
+        c[2, 1] = bad
+        p, _ = _connectivity_file(tmp_path, c)
+        with pytest.raises(H.FvhError):
+            H.read_exodus(p)
+
+
+def test_exodus_reader_survives_malformed_files(tmp_path):
+    """Truncated files and random corruption of the header are read or refused,
+    never crash (checked in a child process)."""
+    import subprocess
+    import sys
+    p, _ = _connectivity_file(tmp_path, None)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "tests", "_exodus_fuzz.py"), p, "7"],
+                       capture_output=True, text=True, timeout=300, cwd=root,
+                       env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
+    assert "refused" in r.stdout
