@@ -34,6 +34,43 @@ Value Table::get(const Value &key) const {
   return it == hash.end() ? Value() : it->second;
 }
 
+// Tables, scopes and closures reference one another through shared_ptr, and a
+// script can chain them arbitrarily deep (t = {t} in a loop, or a closure that
+// captures the previous one).  Freed member by member, such a chain recurses
+// once per link in the destructors and overflows the stack; instead each
+// destructor moves its children to a list that the outermost destructor of the
+// thread empties in a loop.
+namespace {
+thread_local std::vector<std::shared_ptr<void>> *t_release = nullptr;
+
+void take(Value &v, std::vector<std::shared_ptr<void>> &out) {
+  if (v.t) out.push_back(std::move(v.t));
+  if (v.f) out.push_back(std::move(v.f));
+}
+}  // namespace
+
+template <class Collect>
+static void release_children(Collect &&collect) {
+  std::vector<std::shared_ptr<void>> list;
+  const bool outermost = t_release == nullptr;
+  if (outermost) t_release = &list;
+  collect(*t_release);
+  if (!outermost) return;
+  while (!list.empty()) {
+    std::shared_ptr<void> p = std::move(list.back());
+    list.pop_back();
+    p.reset();  // may append this object's own children to the list
+  }
+  t_release = nullptr;
+}
+
+Table::~Table() {
+  release_children([this](std::vector<std::shared_ptr<void>> &out) {
+    for (auto &v : array) take(v, out);
+    for (auto &kv : hash) take(kv.second, out);
+  });
+}
+
 void Table::set(const Value &key, const Value &v) {
   if (key.kind == Value::NUMBER && key.n >= 1 && key.n == std::floor(key.n) &&
       key.n <= (double)array.size() + 1) {
@@ -258,6 +295,24 @@ class Parser {
   std::string name_;
   size_t p_ = 0;
 
+  // Depth of the tree along the current path: one level per block() or expr()
+  // in progress and one per operator or suffix folded into a left-deep chain
+  // (a + b + c ..., a.b.c ...).  The bound keeps the parser's own recursion,
+  // and the recursion of the evaluator and of the tree's destruction, within a
+  // small part of the thread's stack.
+  static constexpr int kMaxDepth = 1000;
+  int depth_ = 0;
+  struct Deeper {
+    Parser &p;
+    int levels = 0;
+    explicit Deeper(Parser &parser) : p(parser) { add(); }
+    void add() {
+      ++levels;
+      if (++p.depth_ > kMaxDepth) p.fail("chunk has too many syntax levels");
+    }
+    ~Deeper() { p.depth_ -= levels; }
+  };
+
   const Token &cur() const { return t_[p_]; }
   [[noreturn]] void fail(const std::string &m) const {
     throw Error(name_ + ":" + std::to_string(cur().line) + ": " + m);
@@ -283,6 +338,7 @@ class Parser {
   }
 
   NodeP block() {
+    Deeper guard(*this);
     auto b = std::make_unique<Node>(S_BLOCK, cur().line);
     while (!block_end()) {
       if (kw("return")) {
@@ -472,9 +528,11 @@ class Parser {
   }
 
   NodeP suffixed() {
+    Deeper guard(*this);
     NodeP e = primary();
     for (;;) {
       const int line = cur().line;
+      if (sym(".") || sym("[") || sym("(") || sym("{") || cur().type == T_STRING) guard.add();
       if (sym(".")) {
         ++p_;
         auto idx = std::make_unique<Node>(E_INDEX, line);
@@ -594,6 +652,7 @@ class Parser {
   }
 
   NodeP expr(int limit = 0) {
+    Deeper guard(*this);
     NodeP left;
     const int line = cur().line;
     if (kw("not") || sym("-") || sym("#")) {
@@ -607,6 +666,7 @@ class Parser {
     }
     for (std::string op = binop(); !op.empty() && left_prio(op) > limit; op = binop()) {
       ++p_;
+      guard.add();
       NodeP right = expr(right_prio(op));
       auto b = std::make_unique<Node>(op == "and" ? E_AND : op == "or" ? E_OR : E_BINARY, line);
       b->text = op;
@@ -626,6 +686,12 @@ class Parser {
 struct Scope {
   std::map<std::string, Value> vars;
   std::shared_ptr<Scope> parent;
+  ~Scope() {
+    release_children([this](std::vector<std::shared_ptr<void>> &out) {
+      for (auto &kv : vars) take(kv.second, out);
+      if (parent) out.push_back(std::move(parent));
+    });
+  }
 };
 using ScopeP = std::shared_ptr<Scope>;
 
@@ -633,13 +699,31 @@ struct Function {
   const Node *def = nullptr;  // E_FUNCTION node (owned by the State)
   ScopeP closure;
   std::function<std::vector<Value>(const std::vector<Value> &)> builtin;
+  ~Function() {
+    release_children([this](std::vector<std::shared_ptr<void>> &out) {
+      if (closure) out.push_back(std::move(closure));
+    });
+  }
 };
 
 struct State::Impl {
   std::vector<NodeP> chunks;
   TablePtr globals = std::make_shared<Table>();
   std::string chunk_name;
-  int depth = 0;
+  // Nested Lua calls (Lua's own limit is 200 C levels) and nested eval()/exec()
+  // frames (each a few hundred bytes of native stack), both restored when an
+  // error unwinds them.
+  static constexpr int kMaxCalls = 200;
+  static constexpr int kMaxFrames = 3000;
+  int depth = 0, frames = 0;
+  struct Enter {
+    int &count;
+    Enter(const Impl &s, int &c, int limit, const Node *n) : count(c) {
+      if (count >= limit) s.fail(n, "stack overflow");
+      ++count;
+    }
+    ~Enter() { --count; }
+  };
 
   enum Flow { NORMAL, RETURN, BREAK };
 
@@ -668,7 +752,7 @@ struct State::Impl {
   std::vector<Value> call(const Node *n, const Value &fn, const std::vector<Value> &args) {
     if (fn.kind != Value::FUNCTION) fail(n, "attempt to call a non-function value");
     if (fn.f->builtin) return fn.f->builtin(args);
-    if (++depth > 200) fail(n, "stack overflow");
+    Enter call_level(*this, depth, kMaxCalls, n);
     auto sc = std::make_shared<Scope>();
     sc->parent = fn.f->closure;
     const Node *def = fn.f->def;
@@ -676,7 +760,6 @@ struct State::Impl {
       sc->vars[def->names[i]] = i < args.size() ? args[i] : Value();
     std::vector<Value> ret;
     exec_block(def->kids[0].get(), sc, ret);
-    --depth;
     return ret;
   }
 
@@ -726,6 +809,7 @@ struct State::Impl {
   }
 
   Value eval(const Node *n, const ScopeP &sc) {
+    Enter frame(*this, frames, kMaxFrames, n);
     switch (n->kind) {
       case E_NIL: return Value();
       case E_TRUE: return Value::boolean(true);
@@ -848,6 +932,7 @@ struct State::Impl {
   }
 
   Flow exec(const Node *s, ScopeP &sc, std::vector<Value> &ret) {
+    Enter frame(*this, frames, kMaxFrames, s);
     switch (s->kind) {
       case S_LOCAL: {
         if (!s->kids.empty() && s->kids[0]->kind == E_FUNCTION && s->names.size() == 1 &&

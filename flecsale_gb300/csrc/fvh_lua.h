@@ -55,6 +55,7 @@ struct Value {
 struct Table {
   std::vector<Value> array;            // t[1..n]
   std::map<std::string, Value> hash;   // string keys (and non-sequence numeric keys as text)
+  ~Table();  // frees nested tables and closures without recursing per level
   Value get(const Value &key) const;
   void set(const Value &key, const Value &v);
 };

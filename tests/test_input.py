@@ -118,3 +118,62 @@ def test_driver_options():
     assert r.returncode == 2
     r = subprocess.run([drv, "-f", "/nonexistent.lua"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+_HOSTILE = r'''
+import sys
+import flecsale_gb300.hydro as H
+
+def load(text):
+    try:
+        H.Input(text=text + "\nhydro = {}").close()
+        return "ok"
+    except H.FvhError as e:
+        return "error: " + str(e)[:60]
+
+n = 200000
+cases = {
+    "parens": "x = " + "(" * n + "1" + ")" * n,
+    "unary": "x = " + "- " * n + "1",
+    "sum": "x = 1" + " + 1" * n,
+    "power": "x = 2" + " ^ 1" * n,
+    "concat": "x = 'a'" + " .. 'a'" * n,
+    "suffix": "t = {} x = t" + ".a" * n,
+    "calls": "f = function() return f end x = f" + "()" * n,
+    "tables": "x = " + "{" * n + "}" * n,
+    "blocks": "do " * n + "end " * n,
+    "functions": "x = " + "function() return " * 5000 + "1" + " end" * 5000,
+    "recursion": "function f(k) return f(k + 1) end f(1)",
+    "deep_body": "function f(k) if k > 0 then return " + "(" * 400 + "f(k - 1)" + ")" * 400
+                 + " end return 0 end x = f(150)",
+}
+# data chains built at run time are freed without recursing per link
+runtime = {
+    "table_chain": "local t = {} for i = 1, 300000 do t = {t} end x = t",
+    "closure_chain": "local f = nil for i = 1, 300000 do local g = f f = function() return g end end x = f",
+    "many_locals": "local a = 1\n" * 100000 + "x = a",
+}
+for name, text in list(cases.items()) + list(runtime.items()):
+    print(name, load(text), flush=True)
+print("survived")
+'''
+
+
+def test_hostile_inputs_are_refused_not_crashed():
+    """Nesting far beyond any input file (parentheses, operator and suffix
+    chains, tables, blocks, recursion) is refused with an error, and long
+    chains of tables or closures built at run time are freed without
+    overflowing the native stack (checked in a child process)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([os.sys.executable, "-c", _HOSTILE], capture_output=True, text=True,
+                       timeout=600, cwd=root, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0 and "survived" in r.stdout, (r.returncode, r.stdout[-3000:],
+                                                          r.stderr[-3000:])
+    lines = dict(l.split(" ", 1) for l in r.stdout.splitlines() if " " in l)
+    for name in ("parens", "unary", "sum", "power", "concat", "suffix", "calls", "tables",
+                 "blocks", "functions"):
+        assert "too many syntax levels" in lines[name], (name, lines[name])
+    for name in ("recursion", "deep_body"):
+        assert "stack overflow" in lines[name], (name, lines[name])
+    for name in ("table_chain", "closure_chain", "many_locals"):
+        assert lines[name] == "ok", (name, lines[name])
