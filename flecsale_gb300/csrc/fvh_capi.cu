@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
@@ -256,64 +257,66 @@ void fvh_solver_destroy(fvh_solver *s) {
 
 fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params,
                              fvh_solver **out) {
-  if (!out || !mesh_ok(mesh) || !params_ok(params, mesh->dim)) return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  fvh_solver *s = new (std::nothrow) fvh_solver();
-  if (!s) return FVH_ERR_OUT_OF_MEMORY;
-  s->mesh = *mesh;
-  s->params = *params;
-  const int D = mesh->dim;
-  const size_t nc = mesh->num_cells, nf = mesh->num_faces;
-  const size_t ng = (size_t)(D + 4) * D;
-  cudaError_t e = cudaSuccess;
-  if (params->precision == FVH_PRECISION_FP64) {
-    e = cudaMalloc(&s->work, sizeof(double) * (ng * nc + (size_t)(D + 2) * nf));
-    if (e == cudaSuccess) {
-      double *b = s->work;
-      for (int i = 0; i < D; ++i, b += nc) s->grads.density[i] = b;
-      for (int d = 0; d < D; ++d)
-        for (int i = 0; i < D; ++i, b += nc) s->grads.velocity[d][i] = b;
-      for (int i = 0; i < D; ++i, b += nc) s->grads.internal_energy[i] = b;
-      for (int i = 0; i < D; ++i, b += nc) s->grads.pressure[i] = b;
-      for (int i = 0; i < D; ++i, b += nc) s->grads.sound_speed[i] = b;
-      s->flux.mass = b;
-      b += nf;
-      for (int i = 0; i < D; ++i, b += nf) s->flux.momentum[i] = b;
-      s->flux.energy = b;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!out || !mesh_ok(mesh) || !params_ok(params, mesh->dim)) return FVH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    fvh_solver *s = new (std::nothrow) fvh_solver();
+    if (!s) return FVH_ERR_OUT_OF_MEMORY;
+    s->mesh = *mesh;
+    s->params = *params;
+    const int D = mesh->dim;
+    const size_t nc = mesh->num_cells, nf = mesh->num_faces;
+    const size_t ng = (size_t)(D + 4) * D;
+    cudaError_t e = cudaSuccess;
+    if (params->precision == FVH_PRECISION_FP64) {
+      e = cudaMalloc(&s->work, sizeof(double) * (ng * nc + (size_t)(D + 2) * nf));
+      if (e == cudaSuccess) {
+        double *b = s->work;
+        for (int i = 0; i < D; ++i, b += nc) s->grads.density[i] = b;
+        for (int d = 0; d < D; ++d)
+          for (int i = 0; i < D; ++i, b += nc) s->grads.velocity[d][i] = b;
+        for (int i = 0; i < D; ++i, b += nc) s->grads.internal_energy[i] = b;
+        for (int i = 0; i < D; ++i, b += nc) s->grads.pressure[i] = b;
+        for (int i = 0; i < D; ++i, b += nc) s->grads.sound_speed[i] = b;
+        s->flux.mass = b;
+        b += nf;
+        for (int i = 0; i < D; ++i, b += nf) s->flux.momentum[i] = b;
+        s->flux.energy = b;
+      }
+      // geometry-only tables (built once, same arithmetic as on the fly)
+      int32_t nnz = 0;
+      if (e == cudaSuccess)
+        e = cudaMemcpy(&nnz, mesh->cell_face_offsets + nc, sizeof(int32_t), cudaMemcpyDeviceToHost);
+      const size_t nlsq = (size_t)fvh::plain::lsq_doubles_per_cell(D) * nc;
+      if (e == cudaSuccess) e = cudaMalloc(&s->tables, sizeof(double) * (nlsq + (size_t)nnz + 1));
+      if (e == cudaSuccess) {
+        s->lsq = s->tables;
+        s->slot_dx = s->tables + nlsq;
+        e = D == 2 ? fvh::plain::build_tables<2>(*mesh, s->lsq, s->slot_dx)
+                   : fvh::plain::build_tables<3>(*mesh, s->lsq, s->slot_dx);
+      }
+    } else {
+      const fvh_status ms = fvh::mixed::create(*mesh, *params, &s->mixed);
+      if (ms != FVH_OK) {
+        fvh_solver_destroy(s);
+        return ms;
+      }
     }
-    // geometry-only tables (built once, same arithmetic as on the fly)
-    int32_t nnz = 0;
     if (e == cudaSuccess)
-      e = cudaMemcpy(&nnz, mesh->cell_face_offsets + nc, sizeof(int32_t), cudaMemcpyDeviceToHost);
-    const size_t nlsq = (size_t)fvh::plain::lsq_doubles_per_cell(D) * nc;
-    if (e == cudaSuccess) e = cudaMalloc(&s->tables, sizeof(double) * (nlsq + (size_t)nnz + 1));
-    if (e == cudaSuccess) {
-      s->lsq = s->tables;
-      s->slot_dx = s->tables + nlsq;
-      e = D == 2 ? fvh::plain::build_tables<2>(*mesh, s->lsq, s->slot_dx)
-                 : fvh::plain::build_tables<3>(*mesh, s->lsq, s->slot_dx);
-    }
-  } else {
-    const fvh_status ms = fvh::mixed::create(*mesh, *params, &s->mixed);
-    if (ms != FVH_OK) {
+      e = cudaMalloc(&s->scalars, sizeof(double) * 2 + fvh_time_step_workspace_bytes(mesh->num_cells));
+    if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(fvh_device_status));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->host_scalars, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->host_status, sizeof(fvh_device_status));
+    if (e == cudaSuccess) e = cudaMemset(s->scalars, 0, sizeof(double) * 2);
+    if (e == cudaSuccess) e = cudaMemset(s->status, 0xff, sizeof(fvh_device_status));
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
       fvh_solver_destroy(s);
-      return ms;
+      return from_cuda(e);
     }
-  }
-  if (e == cudaSuccess)
-    e = cudaMalloc(&s->scalars, sizeof(double) * 2 + fvh_time_step_workspace_bytes(mesh->num_cells));
-  if (e == cudaSuccess) e = cudaMalloc(&s->status, sizeof(fvh_device_status));
-  if (e == cudaSuccess) e = cudaMallocHost(&s->host_scalars, sizeof(double) * 2);
-  if (e == cudaSuccess) e = cudaMallocHost(&s->host_status, sizeof(fvh_device_status));
-  if (e == cudaSuccess) e = cudaMemset(s->scalars, 0, sizeof(double) * 2);
-  if (e == cudaSuccess) e = cudaMemset(s->status, 0xff, sizeof(fvh_device_status));
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) {
-    fvh_solver_destroy(s);
-    return from_cuda(e);
-  }
-  *out = s;
-  return FVH_OK;
+    *out = s;
+    return FVH_OK;
+  });
 }
 
 static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state,
@@ -536,48 +539,51 @@ void profile_mark(void *vctx, const char *name) {
 fvh_status fvh_solver_profile(fvh_solver *s, const fvh_state_view *state, int32_t nsteps,
                               int32_t max_kernels, const char **names, double *mean_ms,
                               int32_t *launches, int32_t *nkernels, fvh_stream_t stream) {
-  if (!s || !state_ok(state, s->mesh.dim) || nsteps <= 0 || max_kernels <= 0 || !names ||
-      !mean_ms || !launches || !nkernels)
-    return FVH_ERR_INVALID_ARGUMENT;
-  profile_ctx ctx;
-  ctx.st = cs(stream);
-  const size_t nev = (size_t)nsteps * 16 + 1;
-  ctx.events.resize(nev);
-  for (auto &e : ctx.events) cudaEventCreate(&e);
-  fvh::mixed::launch_mark mark;
-  mark.fn = profile_mark;
-  mark.ctx = &ctx;
-  fvh_status r = FVH_OK;
-  profile_mark(&ctx, "");  // start event
-  for (int k = 0; k < nsteps && r == FVH_OK; ++k)
-    r = solver_step_enqueue(s, state, ctx.st, mark, chunk_flags(k, nsteps));
-  if (r == FVH_OK) r = from_cuda(cudaStreamSynchronize(ctx.st));
-  int32_t nk = 0;
-  if (r == FVH_OK) {
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!s || !state_ok(state, s->mesh.dim) || nsteps <= 0 || max_kernels <= 0 || !names ||
+        !mean_ms || !launches || !nkernels)
+      return FVH_ERR_INVALID_ARGUMENT;
+    profile_ctx ctx;
+    ctx.st = cs(stream);
+    const size_t nev = (size_t)nsteps * 16 + 1;
+    ctx.events.resize(nev);
+    ctx.names.reserve(nev);  // profile_mark records at most nev names, without reallocating
     std::vector<double> total(max_kernels, 0.0);
     std::vector<int> count(max_kernels, 0);
-    const size_t recorded = ctx.names.size();
-    for (size_t i = 1; i < recorded; ++i) {
-      float ms = 0;
-      cudaEventElapsedTime(&ms, ctx.events[i - 1], ctx.events[i]);
-      int k = 0;
-      for (; k < nk; ++k)
-        if (std::strcmp(names[k], ctx.names[i]) == 0) break;
-      if (k == nk) {
-        if (nk == max_kernels) continue;
-        names[nk++] = ctx.names[i];
+    for (auto &e : ctx.events) cudaEventCreate(&e);  // nothing below allocates host memory
+    fvh::mixed::launch_mark mark;
+    mark.fn = profile_mark;
+    mark.ctx = &ctx;
+    fvh_status r = FVH_OK;
+    profile_mark(&ctx, "");  // start event
+    for (int k = 0; k < nsteps && r == FVH_OK; ++k)
+      r = solver_step_enqueue(s, state, ctx.st, mark, chunk_flags(k, nsteps));
+    if (r == FVH_OK) r = from_cuda(cudaStreamSynchronize(ctx.st));
+    int32_t nk = 0;
+    if (r == FVH_OK) {
+      const size_t recorded = ctx.names.size();
+      for (size_t i = 1; i < recorded; ++i) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx.events[i - 1], ctx.events[i]);
+        int k = 0;
+        for (; k < nk; ++k)
+          if (std::strcmp(names[k], ctx.names[i]) == 0) break;
+        if (k == nk) {
+          if (nk == max_kernels) continue;
+          names[nk++] = ctx.names[i];
+        }
+        total[k] += ms;
+        count[k]++;
       }
-      total[k] += ms;
-      count[k]++;
+      for (int k = 0; k < nk; ++k) {
+        mean_ms[k] = count[k] ? total[k] / count[k] : 0.0;
+        launches[k] = count[k];
+      }
     }
-    for (int k = 0; k < nk; ++k) {
-      mean_ms[k] = count[k] ? total[k] / count[k] : 0.0;
-      launches[k] = count[k];
-    }
-  }
-  *nkernels = nk;
-  for (auto &e : ctx.events) cudaEventDestroy(e);
-  return r;
+    *nkernels = nk;
+    for (auto &e : ctx.events) cudaEventDestroy(e);
+    return r;
+  });
 }
 
 // One step is a fixed sequence of launches; each variant is captured once per
@@ -695,55 +701,56 @@ void fvh_device_mesh_destroy(fvh_device_mesh *dm) {
 }
 
 fvh_status fvh_device_mesh_create(const fvh_host_mesh *m, fvh_device_mesh **out) {
-  if (!m || !out) return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  fvh_device_mesh *dm = new (std::nothrow) fvh_device_mesh();
-  if (!dm) return FVH_ERR_OUT_OF_MEMORY;
-  cudaError_t e = cudaSuccess;
-  auto up = [&](const void *src, size_t bytes) -> void * {
-    if (e != cudaSuccess) return nullptr;
-    void *d = nullptr;
-    e = cudaMalloc(&d, bytes > 0 ? bytes : 16);
-    if (e != cudaSuccess) return nullptr;
-    dm->allocs.push_back(d);
-    if (bytes) e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
-    return d;
-  };
-  auto upi = [&](const std::vector<int32_t> &v) {
-    return static_cast<const int32_t *>(up(v.data(), v.size() * sizeof(int32_t)));
-  };
-  auto upd = [&](const std::vector<double> &v) {
-    return static_cast<const double *>(up(v.data(), v.size() * sizeof(double)));
-  };
-  fvh_mesh_view &o = dm->view;
-  dm->nnz_cf = (int32_t)m->cf.size();
-  dm->nnz_nb = (int32_t)m->nb.size();
-  dm->nnz_cv = (int32_t)m->cv.size();
-  o.dim = m->dim;
-  o.num_cells = m->nc;
-  o.num_faces = m->nf;
-  o.num_vertices = m->nv;
-  o.face_cells = upi(m->face_cells);
-  o.cell_face_offsets = upi(m->cf_off);
-  o.cell_faces = upi(m->cf);
-  o.cell_nbr_offsets = upi(m->nb_off);
-  o.cell_nbrs = upi(m->nb);
-  o.cell_vertex_offsets = upi(m->cv_off);
-  o.cell_vertices = upi(m->cv);
-  for (int d = 0; d < m->dim; ++d) {
-    o.cell_centroid[d] = upd(m->cc[d]);
-    o.face_centroid[d] = upd(m->fc[d]);
-    o.face_normal[d] = upd(m->fn[d]);
-    o.vertex_coord[d] = upd(m->vc[d]);
-  }
-  o.cell_volume = upd(m->cvol);
-  o.face_area = upd(m->fa);
-  if (e != cudaSuccess) {
-    fvh_device_mesh_destroy(dm);
-    return from_cuda(e);
-  }
-  *out = dm;
-  return FVH_OK;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!m || !out) return FVH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    fvh_device_mesh *dm = new (std::nothrow) fvh_device_mesh();
+    if (!dm) return FVH_ERR_OUT_OF_MEMORY;
+    std::unique_ptr<fvh_device_mesh, void (*)(fvh_device_mesh *)> own(dm, fvh_device_mesh_destroy);
+    dm->allocs.reserve(32);  // at most 21 arrays: recording one never throws
+    cudaError_t e = cudaSuccess;
+    auto up = [&](const void *src, size_t bytes) -> void * {
+      if (e != cudaSuccess) return nullptr;
+      void *d = nullptr;
+      e = cudaMalloc(&d, bytes > 0 ? bytes : 16);
+      if (e != cudaSuccess) return nullptr;
+      dm->allocs.push_back(d);
+      if (bytes) e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
+      return d;
+    };
+    auto upi = [&](const std::vector<int32_t> &v) {
+      return static_cast<const int32_t *>(up(v.data(), v.size() * sizeof(int32_t)));
+    };
+    auto upd = [&](const std::vector<double> &v) {
+      return static_cast<const double *>(up(v.data(), v.size() * sizeof(double)));
+    };
+    fvh_mesh_view &o = dm->view;
+    dm->nnz_cf = (int32_t)m->cf.size();
+    dm->nnz_nb = (int32_t)m->nb.size();
+    dm->nnz_cv = (int32_t)m->cv.size();
+    o.dim = m->dim;
+    o.num_cells = m->nc;
+    o.num_faces = m->nf;
+    o.num_vertices = m->nv;
+    o.face_cells = upi(m->face_cells);
+    o.cell_face_offsets = upi(m->cf_off);
+    o.cell_faces = upi(m->cf);
+    o.cell_nbr_offsets = upi(m->nb_off);
+    o.cell_nbrs = upi(m->nb);
+    o.cell_vertex_offsets = upi(m->cv_off);
+    o.cell_vertices = upi(m->cv);
+    for (int d = 0; d < m->dim; ++d) {
+      o.cell_centroid[d] = upd(m->cc[d]);
+      o.face_centroid[d] = upd(m->fc[d]);
+      o.face_normal[d] = upd(m->fn[d]);
+      o.vertex_coord[d] = upd(m->vc[d]);
+    }
+    o.cell_volume = upd(m->cvol);
+    o.face_area = upd(m->fa);
+    if (e != cudaSuccess) return from_cuda(e);
+    *out = own.release();
+    return FVH_OK;
+  });
 }
 
 const fvh_mesh_view *fvh_device_mesh_view(const fvh_device_mesh *dm) {

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <new>
 #include <vector>
 
 #include "flecsale_gb300.h"
@@ -28,5 +29,21 @@ struct fvh_device_mesh {
 
 namespace fvh {
 fvh_status build_topology_and_geometry(fvh_host_mesh &m);
+
+// Runs the body of a C entry point so that no C++ exception crosses the C ABI:
+// a failed host allocation (std::bad_alloc) becomes FVH_ERR_OUT_OF_MEMORY and
+// any other exception FVH_ERR_INVALID_ARGUMENT.  Objects the body builds are
+// owned by RAII guards until it succeeds, so an exception leaks nothing.
+template <class Body>
+fvh_status no_throw(Body &&body) noexcept {
+  try {
+    return body();
+  } catch (const std::bad_alloc &) {
+    return FVH_ERR_OUT_OF_MEMORY;
+  } catch (...) {
+    return FVH_ERR_INVALID_ARGUMENT;
+  }
+}
+
 double uniform01(uint64_t seed, uint64_t counter);
 }  // namespace fvh

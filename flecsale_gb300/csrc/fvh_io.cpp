@@ -181,98 +181,100 @@ std::string attr(const nc_var &v, const char *n) {
 extern "C" {
 
 fvh_status fvh_host_mesh_read_exodus(const char *path, fvh_host_mesh **out) {
-  if (!path || !out) return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  std::FILE *f = std::fopen(path, "rb");
-  if (!f) return FVH_ERR_INVALID_ARGUMENT;
-  nc_file nc;
-  std::fseek(f, 0, SEEK_END);
-  const long size = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  nc.buf.resize(size > 0 ? (size_t)size : 0);
-  const size_t got = nc.buf.empty() ? 0 : std::fread(nc.buf.data(), 1, nc.buf.size(), f);
-  std::fclose(f);
-  if (got != nc.buf.size() || !nc.parse()) return FVH_ERR_UNSUPPORTED;  // not CDF-1/2
-  // coordinates
-  std::vector<double> xyz[3];
-  int ncoord = 0;
-  const char *cn[3] = {"coordx", "coordy", "coordz"};
-  for (int d = 0; d < 3; ++d)
-    if (const nc_var *v = nc.var(cn[d])) {
-      if (!nc.read_f64(*v, &xyz[d])) return FVH_ERR_UNSUPPORTED;
-      ncoord = d + 1;
-    }
-  if (ncoord == 0) {
-    const nc_var *v = nc.var("coord");
-    std::vector<double> all;
-    if (!v || v->dims.size() != 2 || !nc.read_f64(*v, &all)) return FVH_ERR_UNSUPPORTED;
-    ncoord = (int)nc.dims[v->dims[0]].second;
-    if (ncoord < 2 || ncoord > 3) return FVH_ERR_UNSUPPORTED;
-    const size_t nn = nc.dims[v->dims[1]].second;
-    for (int d = 0; d < ncoord; ++d) xyz[d].assign(all.begin() + d * nn, all.begin() + (d + 1) * nn);
-  }
-  // two or three coordinate arrays, all of one length that int32 ids can index
-  if (ncoord < 2) return FVH_ERR_UNSUPPORTED;
-  const size_t nv = xyz[0].size();
-  if (nv == 0 || nv >= (size_t)INT32_MAX) return FVH_ERR_UNSUPPORTED;
-  for (int d = 1; d < ncoord; ++d)
-    if (xyz[d].size() != nv) return FVH_ERR_UNSUPPORTED;
-  // element blocks connect1, connect2, ...
-  std::vector<int32_t> off{0}, cells;
-  int shape = 0;  // nodes per element of the first block
-  bool shell = false;
-  for (int blk = 1;; ++blk) {
-    const nc_var *v = nc.var("connect" + std::to_string(blk));
-    if (!v) break;
-    std::vector<double> c;
-    if (v->dims.size() != 2 || !nc.read_f64(*v, &c)) return FVH_ERR_UNSUPPORTED;
-    const std::string et = attr(*v, "elem_type");
-    const uint64_t npe64 = nc.dims[v->dims[1]].second;
-    if (npe64 < 3 || npe64 > 8) return FVH_ERR_UNSUPPORTED;
-    const int npe = (int)npe64;
-    if (shape == 0) shape = npe;
-    if (npe != shape) return FVH_ERR_UNSUPPORTED;  // mixed element shapes
-    if (et.rfind("SHELL", 0) == 0) shell = true;
-    if (cells.size() + c.size() >= (size_t)INT32_MAX) return FVH_ERR_CAPACITY;
-    for (size_t k = 0; k + npe <= c.size(); k += npe) {
-      for (int q = 0; q < npe; ++q) {
-        // Exodus node ids are 1-based; anything else is a malformed file
-        const double id = c[k + q];
-        if (!(id >= 1 && id <= (double)nv) || id != std::floor(id))
-          return FVH_ERR_INVALID_ARGUMENT;
-        cells.push_back((int32_t)id - 1);
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!path || !out) return FVH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::FILE *f = std::fopen(path, "rb");
+    if (!f) return FVH_ERR_INVALID_ARGUMENT;
+    nc_file nc;
+    std::fseek(f, 0, SEEK_END);
+    const long size = std::ftell(f);
+    std::fseek(f, 0, SEEK_SET);
+    nc.buf.resize(size > 0 ? (size_t)size : 0);
+    const size_t got = nc.buf.empty() ? 0 : std::fread(nc.buf.data(), 1, nc.buf.size(), f);
+    std::fclose(f);
+    if (got != nc.buf.size() || !nc.parse()) return FVH_ERR_UNSUPPORTED;  // not CDF-1/2
+    // coordinates
+    std::vector<double> xyz[3];
+    int ncoord = 0;
+    const char *cn[3] = {"coordx", "coordy", "coordz"};
+    for (int d = 0; d < 3; ++d)
+      if (const nc_var *v = nc.var(cn[d])) {
+        if (!nc.read_f64(*v, &xyz[d])) return FVH_ERR_UNSUPPORTED;
+        ncoord = d + 1;
       }
-      off.push_back((int32_t)cells.size());
+    if (ncoord == 0) {
+      const nc_var *v = nc.var("coord");
+      std::vector<double> all;
+      if (!v || v->dims.size() != 2 || !nc.read_f64(*v, &all)) return FVH_ERR_UNSUPPORTED;
+      ncoord = (int)nc.dims[v->dims[0]].second;
+      if (ncoord < 2 || ncoord > 3) return FVH_ERR_UNSUPPORTED;
+      const size_t nn = nc.dims[v->dims[1]].second;
+      for (int d = 0; d < ncoord; ++d) xyz[d].assign(all.begin() + d * nn, all.begin() + (d + 1) * nn);
     }
-  }
-  if (cells.empty() || nv == 0) return FVH_ERR_UNSUPPORTED;
-  // dimension: QUAD4/SHELL4 with a flat z are 2D polygons
-  int dim = ncoord;
-  if (shape == 4 && (ncoord == 2 || shell)) {
-    dim = 2;
-    if (ncoord == 3)
-      for (double z : xyz[2])
-        if (std::fabs(z - xyz[2][0]) > 0) return FVH_ERR_UNSUPPORTED;  // curved shell
-  }
-  if (dim == 3 && shape != 8 && shape != 4) return FVH_ERR_UNSUPPORTED;
-  std::vector<double> coords(nv * dim);
-  for (size_t i = 0; i < nv; ++i)
-    for (int d = 0; d < dim; ++d) coords[i * dim + d] = xyz[d][i];
-  // 2D polygons must be counter-clockwise; reverse clockwise ones
-  if (dim == 2) {
-    const size_t ncell = off.size() - 1;
-    for (size_t c = 0; c < ncell; ++c) {
-      double a2 = 0;
-      const int b = off[c], n = off[c + 1] - b;
-      for (int k = 0; k < n; ++k) {
-        const int p = cells[b + k], q = cells[b + (k + 1) % n];
-        a2 += coords[2 * p] * coords[2 * q + 1] - coords[2 * q] * coords[2 * p + 1];
+    // two or three coordinate arrays, all of one length that int32 ids can index
+    if (ncoord < 2) return FVH_ERR_UNSUPPORTED;
+    const size_t nv = xyz[0].size();
+    if (nv == 0 || nv >= (size_t)INT32_MAX) return FVH_ERR_UNSUPPORTED;
+    for (int d = 1; d < ncoord; ++d)
+      if (xyz[d].size() != nv) return FVH_ERR_UNSUPPORTED;
+    // element blocks connect1, connect2, ...
+    std::vector<int32_t> off{0}, cells;
+    int shape = 0;  // nodes per element of the first block
+    bool shell = false;
+    for (int blk = 1;; ++blk) {
+      const nc_var *v = nc.var("connect" + std::to_string(blk));
+      if (!v) break;
+      std::vector<double> c;
+      if (v->dims.size() != 2 || !nc.read_f64(*v, &c)) return FVH_ERR_UNSUPPORTED;
+      const std::string et = attr(*v, "elem_type");
+      const uint64_t npe64 = nc.dims[v->dims[1]].second;
+      if (npe64 < 3 || npe64 > 8) return FVH_ERR_UNSUPPORTED;
+      const int npe = (int)npe64;
+      if (shape == 0) shape = npe;
+      if (npe != shape) return FVH_ERR_UNSUPPORTED;  // mixed element shapes
+      if (et.rfind("SHELL", 0) == 0) shell = true;
+      if (cells.size() + c.size() >= (size_t)INT32_MAX) return FVH_ERR_CAPACITY;
+      for (size_t k = 0; k + npe <= c.size(); k += npe) {
+        for (int q = 0; q < npe; ++q) {
+          // Exodus node ids are 1-based; anything else is a malformed file
+          const double id = c[k + q];
+          if (!(id >= 1 && id <= (double)nv) || id != std::floor(id))
+            return FVH_ERR_INVALID_ARGUMENT;
+          cells.push_back((int32_t)id - 1);
+        }
+        off.push_back((int32_t)cells.size());
       }
-      if (a2 < 0) std::reverse(cells.begin() + b + 1, cells.begin() + b + n);
     }
-  }
-  return fvh_host_mesh_create(dim, (int32_t)nv, coords.data(), (int32_t)(off.size() - 1),
-                              off.data(), cells.data(), out);
+    if (cells.empty() || nv == 0) return FVH_ERR_UNSUPPORTED;
+    // dimension: QUAD4/SHELL4 with a flat z are 2D polygons
+    int dim = ncoord;
+    if (shape == 4 && (ncoord == 2 || shell)) {
+      dim = 2;
+      if (ncoord == 3)
+        for (double z : xyz[2])
+          if (std::fabs(z - xyz[2][0]) > 0) return FVH_ERR_UNSUPPORTED;  // curved shell
+    }
+    if (dim == 3 && shape != 8 && shape != 4) return FVH_ERR_UNSUPPORTED;
+    std::vector<double> coords(nv * dim);
+    for (size_t i = 0; i < nv; ++i)
+      for (int d = 0; d < dim; ++d) coords[i * dim + d] = xyz[d][i];
+    // 2D polygons must be counter-clockwise; reverse clockwise ones
+    if (dim == 2) {
+      const size_t ncell = off.size() - 1;
+      for (size_t c = 0; c < ncell; ++c) {
+        double a2 = 0;
+        const int b = off[c], n = off[c + 1] - b;
+        for (int k = 0; k < n; ++k) {
+          const int p = cells[b + k], q = cells[b + (k + 1) % n];
+          a2 += coords[2 * p] * coords[2 * q + 1] - coords[2 * q] * coords[2 * p + 1];
+        }
+        if (a2 < 0) std::reverse(cells.begin() + b + 1, cells.begin() + b + n);
+      }
+    }
+    return fvh_host_mesh_create(dim, (int32_t)nv, coords.data(), (int32_t)(off.size() - 1),
+                                off.data(), cells.data(), out);
+  });
 }
 
 fvh_status fvh_dump_write(const char *path, const fvh_host_mesh *m, const double *host_planes,

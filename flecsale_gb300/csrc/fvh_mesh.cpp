@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
@@ -394,149 +395,146 @@ fvh_status fvh_host_mesh_create(int32_t dim, int32_t num_vertices,
                                 const int32_t *cell_vertex_offsets,
                                 const int32_t *cell_vertices,
                                 fvh_host_mesh **out) {
-  if (!out || (dim != 2 && dim != 3) || num_vertices <= 0 || num_cells <= 0 ||
-      !vertex_coords || !cell_vertex_offsets || !cell_vertices)
-    return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  fvh_host_mesh *m = new (std::nothrow) fvh_host_mesh();
-  if (!m) return FVH_ERR_OUT_OF_MEMORY;
-  m->dim = dim;
-  m->nv = num_vertices;
-  m->nc = num_cells;
-  for (int d = 0; d < 3; ++d) m->vc[d].assign(d < dim ? num_vertices : 0, 0.0);
-  for (int v = 0; v < num_vertices; ++v)
-    for (int d = 0; d < dim; ++d) m->vc[d][v] = vertex_coords[(size_t)v * dim + d];
-  m->cv_off.assign(cell_vertex_offsets, cell_vertex_offsets + num_cells + 1);
-  if (m->cv_off[0] != 0) {
-    delete m;
-    return FVH_ERR_INVALID_ARGUMENT;
-  }
-  for (int c = 0; c < num_cells; ++c)
-    if (m->cv_off[c + 1] <= m->cv_off[c]) {
-      delete m;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!out || (dim != 2 && dim != 3) || num_vertices <= 0 || num_cells <= 0 ||
+        !vertex_coords || !cell_vertex_offsets || !cell_vertices)
       return FVH_ERR_INVALID_ARGUMENT;
-    }
-  m->cv.assign(cell_vertices, cell_vertices + m->cv_off[num_cells]);
-  const fvh_status st = fvh::build_topology_and_geometry(*m);
-  if (st != FVH_OK) {
-    delete m;
-    return st;
-  }
-  *out = m;
-  return FVH_OK;
+    *out = nullptr;
+    std::unique_ptr<fvh_host_mesh> m(new (std::nothrow) fvh_host_mesh());
+    if (!m) return FVH_ERR_OUT_OF_MEMORY;
+    m->dim = dim;
+    m->nv = num_vertices;
+    m->nc = num_cells;
+    for (int d = 0; d < 3; ++d) m->vc[d].assign(d < dim ? num_vertices : 0, 0.0);
+    for (int v = 0; v < num_vertices; ++v)
+      for (int d = 0; d < dim; ++d) m->vc[d][v] = vertex_coords[(size_t)v * dim + d];
+    m->cv_off.assign(cell_vertex_offsets, cell_vertex_offsets + num_cells + 1);
+    if (m->cv_off[0] != 0) return FVH_ERR_INVALID_ARGUMENT;
+    for (int c = 0; c < num_cells; ++c)
+      if (m->cv_off[c + 1] <= m->cv_off[c]) return FVH_ERR_INVALID_ARGUMENT;
+    m->cv.assign(cell_vertices, cell_vertices + m->cv_off[num_cells]);
+    const fvh_status st = fvh::build_topology_and_geometry(*m);
+    if (st != FVH_OK) return st;
+    *out = m.release();
+    return FVH_OK;
+  });
 }
 
 fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
                              const double *hi, double jitter, uint64_t seed,
                              fvh_host_mesh **out) {
-  if (!out || !n || !lo || !hi || (dim != 2 && dim != 3) || jitter < 0 ||
-      jitter >= 0.5)
-    return FVH_ERR_INVALID_ARGUMENT;
-  int64_t nvx[3] = {1, 1, 1}, ncx[3] = {1, 1, 1};
-  double h[3] = {0, 0, 0};
-  for (int d = 0; d < dim; ++d) {
-    if (n[d] <= 0 || !(hi[d] > lo[d])) return FVH_ERR_INVALID_ARGUMENT;
-    ncx[d] = n[d];
-    nvx[d] = n[d] + 1;
-    h[d] = (hi[d] - lo[d]) / n[d];
-  }
-  const int64_t nv = nvx[0] * nvx[1] * nvx[2];
-  const int64_t nc = ncx[0] * ncx[1] * ncx[2];
-  if (nv >= INT32_MAX || nc * (dim == 2 ? 4 : 8) >= INT32_MAX)
-    return FVH_ERR_CAPACITY;
-  std::vector<double> xyz((size_t)nv * dim);
-#pragma omp parallel for schedule(static)
-  for (int64_t v = 0; v < nv; ++v) {
-    const int64_t idx[3] = {v % nvx[0], (v / nvx[0]) % nvx[1], v / (nvx[0] * nvx[1])};
-    bool boundary = false;
-    for (int d = 0; d < dim; ++d)
-      if (idx[d] == 0 || idx[d] == nvx[d] - 1) boundary = true;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!out || !n || !lo || !hi || (dim != 2 && dim != 3) || jitter < 0 ||
+        jitter >= 0.5)
+      return FVH_ERR_INVALID_ARGUMENT;
+    int64_t nvx[3] = {1, 1, 1}, ncx[3] = {1, 1, 1};
+    double h[3] = {0, 0, 0};
     for (int d = 0; d < dim; ++d) {
-      double x = idx[d] == nvx[d] - 1 ? hi[d] : lo[d] + (double)idx[d] * h[d];
-      if (!boundary && jitter > 0)
-        x += (2.0 * fvh::uniform01(seed, (uint64_t)v * 3 + d) - 1.0) * jitter * h[d];
-      xyz[(size_t)v * dim + d] = x;
+      if (n[d] <= 0 || !(hi[d] > lo[d])) return FVH_ERR_INVALID_ARGUMENT;
+      ncx[d] = n[d];
+      nvx[d] = n[d] + 1;
+      h[d] = (hi[d] - lo[d]) / n[d];
     }
-  }
-  const int per = dim == 2 ? 4 : 8;
-  std::vector<int32_t> off((size_t)nc + 1), cv((size_t)nc * per);
+    const int64_t nv = nvx[0] * nvx[1] * nvx[2];
+    const int64_t nc = ncx[0] * ncx[1] * ncx[2];
+    if (nv >= INT32_MAX || nc * (dim == 2 ? 4 : 8) >= INT32_MAX)
+      return FVH_ERR_CAPACITY;
+    std::vector<double> xyz((size_t)nv * dim);
 #pragma omp parallel for schedule(static)
-  for (int64_t c = 0; c < nc; ++c) {
-    const int64_t i = c % ncx[0], j = (c / ncx[0]) % ncx[1], k = c / (ncx[0] * ncx[1]);
-    auto vid = [&](int64_t a, int64_t b, int64_t cc) {
-      return (int32_t)(a + nvx[0] * (b + nvx[1] * cc));
-    };
-    int32_t *o = cv.data() + c * per;
-    o[0] = vid(i, j, k);
-    o[1] = vid(i + 1, j, k);
-    o[2] = vid(i + 1, j + 1, k);
-    o[3] = vid(i, j + 1, k);
-    if (dim == 3) {
-      o[4] = vid(i, j, k + 1);
-      o[5] = vid(i + 1, j, k + 1);
-      o[6] = vid(i + 1, j + 1, k + 1);
-      o[7] = vid(i, j + 1, k + 1);
+    for (int64_t v = 0; v < nv; ++v) {
+      const int64_t idx[3] = {v % nvx[0], (v / nvx[0]) % nvx[1], v / (nvx[0] * nvx[1])};
+      bool boundary = false;
+      for (int d = 0; d < dim; ++d)
+        if (idx[d] == 0 || idx[d] == nvx[d] - 1) boundary = true;
+      for (int d = 0; d < dim; ++d) {
+        double x = idx[d] == nvx[d] - 1 ? hi[d] : lo[d] + (double)idx[d] * h[d];
+        if (!boundary && jitter > 0)
+          x += (2.0 * fvh::uniform01(seed, (uint64_t)v * 3 + d) - 1.0) * jitter * h[d];
+        xyz[(size_t)v * dim + d] = x;
+      }
     }
-    off[c] = (int32_t)(c * per);
-  }
-  off[nc] = (int32_t)(nc * per);
-  return fvh_host_mesh_create(dim, (int32_t)nv, xyz.data(), (int32_t)nc,
-                              off.data(), cv.data(), out);
+    const int per = dim == 2 ? 4 : 8;
+    std::vector<int32_t> off((size_t)nc + 1), cv((size_t)nc * per);
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nc; ++c) {
+      const int64_t i = c % ncx[0], j = (c / ncx[0]) % ncx[1], k = c / (ncx[0] * ncx[1]);
+      auto vid = [&](int64_t a, int64_t b, int64_t cc) {
+        return (int32_t)(a + nvx[0] * (b + nvx[1] * cc));
+      };
+      int32_t *o = cv.data() + c * per;
+      o[0] = vid(i, j, k);
+      o[1] = vid(i + 1, j, k);
+      o[2] = vid(i + 1, j + 1, k);
+      o[3] = vid(i, j + 1, k);
+      if (dim == 3) {
+        o[4] = vid(i, j, k + 1);
+        o[5] = vid(i + 1, j, k + 1);
+        o[6] = vid(i + 1, j + 1, k + 1);
+        o[7] = vid(i, j + 1, k + 1);
+      }
+      off[c] = (int32_t)(c * per);
+    }
+    off[nc] = (int32_t)(nc * per);
+    return fvh_host_mesh_create(dim, (int32_t)nv, xyz.data(), (int32_t)nc,
+                                off.data(), cv.data(), out);
+  });
 }
 
 void fvh_host_mesh_destroy(fvh_host_mesh *m) { delete m; }
 
 fvh_status fvh_host_mesh_concat(int32_t n, const fvh_host_mesh *const *meshes,
                                 fvh_host_mesh **out) {
-  if (!out || n <= 0 || !meshes) return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  const int dim = meshes[0] ? meshes[0]->dim : 0;
-  int64_t nc = 0, nf = 0, nv = 0, ncf = 0, nnb = 0, ncv = 0, nfv = 0;
-  for (int k = 0; k < n; ++k) {
-    const fvh_host_mesh *m = meshes[k];
-    if (!m || m->dim != dim) return FVH_ERR_INVALID_ARGUMENT;
-    nc += m->nc; nf += m->nf; nv += m->nv;
-    ncf += m->cf.size(); nnb += m->nb.size(); ncv += m->cv.size(); nfv += m->fv.size();
-  }
-  if (nc >= INT32_MAX || nf >= INT32_MAX || nv >= INT32_MAX || ncf >= INT32_MAX ||
-      nnb >= INT32_MAX || ncv >= INT32_MAX || nfv >= INT32_MAX)
-    return FVH_ERR_CAPACITY;
-  fvh_host_mesh *o = new (std::nothrow) fvh_host_mesh();
-  if (!o) return FVH_ERR_OUT_OF_MEMORY;
-  o->dim = dim;
-  o->nc = (int)nc; o->nf = (int)nf; o->nv = (int)nv;
-  o->cf_off.assign(1, 0); o->nb_off.assign(1, 0); o->cv_off.assign(1, 0); o->fv_off.assign(1, 0);
-  int32_t co = 0, fo = 0, vo = 0;
-  for (int k = 0; k < n; ++k) {
-    const fvh_host_mesh &m = *meshes[k];
-    for (int f = 0; f < m.nf; ++f) {
-      const int32_t a = m.face_cells[2 * (size_t)f], b = m.face_cells[2 * (size_t)f + 1];
-      o->face_cells.push_back(a + co);
-      o->face_cells.push_back(b < 0 ? -1 : b + co);
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!out || n <= 0 || !meshes) return FVH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    const int dim = meshes[0] ? meshes[0]->dim : 0;
+    int64_t nc = 0, nf = 0, nv = 0, ncf = 0, nnb = 0, ncv = 0, nfv = 0;
+    for (int k = 0; k < n; ++k) {
+      const fvh_host_mesh *m = meshes[k];
+      if (!m || m->dim != dim) return FVH_ERR_INVALID_ARGUMENT;
+      nc += m->nc; nf += m->nf; nv += m->nv;
+      ncf += m->cf.size(); nnb += m->nb.size(); ncv += m->cv.size(); nfv += m->fv.size();
     }
-    auto append_csr = [](std::vector<int32_t> &off, std::vector<int32_t> &dst,
-                         const std::vector<int32_t> &soff, const std::vector<int32_t> &src,
-                         auto shift) {
-      const int32_t base = off.back();
-      for (size_t i = 1; i < soff.size(); ++i) off.push_back(base + soff[i]);
-      for (int32_t x : src) dst.push_back(shift(x));
-    };
-    append_csr(o->cf_off, o->cf, m.cf_off, m.cf, [fo](int32_t f) { return f >= 0 ? f + fo : ~(~f + fo); });
-    append_csr(o->nb_off, o->nb, m.nb_off, m.nb, [co](int32_t c) { return c + co; });
-    append_csr(o->cv_off, o->cv, m.cv_off, m.cv, [vo](int32_t v) { return v + vo; });
-    append_csr(o->fv_off, o->fv, m.fv_off, m.fv, [vo](int32_t v) { return v + vo; });
-    for (int d = 0; d < 3; ++d) {
-      o->cc[d].insert(o->cc[d].end(), m.cc[d].begin(), m.cc[d].end());
-      o->fc[d].insert(o->fc[d].end(), m.fc[d].begin(), m.fc[d].end());
-      o->fn[d].insert(o->fn[d].end(), m.fn[d].begin(), m.fn[d].end());
-      o->vc[d].insert(o->vc[d].end(), m.vc[d].begin(), m.vc[d].end());
+    if (nc >= INT32_MAX || nf >= INT32_MAX || nv >= INT32_MAX || ncf >= INT32_MAX ||
+        nnb >= INT32_MAX || ncv >= INT32_MAX || nfv >= INT32_MAX)
+      return FVH_ERR_CAPACITY;
+    std::unique_ptr<fvh_host_mesh> o(new (std::nothrow) fvh_host_mesh());
+    if (!o) return FVH_ERR_OUT_OF_MEMORY;
+    o->dim = dim;
+    o->nc = (int)nc; o->nf = (int)nf; o->nv = (int)nv;
+    o->cf_off.assign(1, 0); o->nb_off.assign(1, 0); o->cv_off.assign(1, 0); o->fv_off.assign(1, 0);
+    int32_t co = 0, fo = 0, vo = 0;
+    for (int k = 0; k < n; ++k) {
+      const fvh_host_mesh &m = *meshes[k];
+      for (int f = 0; f < m.nf; ++f) {
+        const int32_t a = m.face_cells[2 * (size_t)f], b = m.face_cells[2 * (size_t)f + 1];
+        o->face_cells.push_back(a + co);
+        o->face_cells.push_back(b < 0 ? -1 : b + co);
+      }
+      auto append_csr = [](std::vector<int32_t> &off, std::vector<int32_t> &dst,
+                           const std::vector<int32_t> &soff, const std::vector<int32_t> &src,
+                           auto shift) {
+        const int32_t base = off.back();
+        for (size_t i = 1; i < soff.size(); ++i) off.push_back(base + soff[i]);
+        for (int32_t x : src) dst.push_back(shift(x));
+      };
+      append_csr(o->cf_off, o->cf, m.cf_off, m.cf, [fo](int32_t f) { return f >= 0 ? f + fo : ~(~f + fo); });
+      append_csr(o->nb_off, o->nb, m.nb_off, m.nb, [co](int32_t c) { return c + co; });
+      append_csr(o->cv_off, o->cv, m.cv_off, m.cv, [vo](int32_t v) { return v + vo; });
+      append_csr(o->fv_off, o->fv, m.fv_off, m.fv, [vo](int32_t v) { return v + vo; });
+      for (int d = 0; d < 3; ++d) {
+        o->cc[d].insert(o->cc[d].end(), m.cc[d].begin(), m.cc[d].end());
+        o->fc[d].insert(o->fc[d].end(), m.fc[d].begin(), m.fc[d].end());
+        o->fn[d].insert(o->fn[d].end(), m.fn[d].begin(), m.fn[d].end());
+        o->vc[d].insert(o->vc[d].end(), m.vc[d].begin(), m.vc[d].end());
+      }
+      o->cvol.insert(o->cvol.end(), m.cvol.begin(), m.cvol.end());
+      o->fa.insert(o->fa.end(), m.fa.begin(), m.fa.end());
+      co += m.nc; fo += m.nf; vo += m.nv;
     }
-    o->cvol.insert(o->cvol.end(), m.cvol.begin(), m.cvol.end());
-    o->fa.insert(o->fa.end(), m.fa.begin(), m.fa.end());
-    co += m.nc; fo += m.nf; vo += m.nv;
-  }
-  *out = o;
-  return FVH_OK;
+    *out = o.release();
+    return FVH_OK;
+  });
 }
 
 fvh_status fvh_host_mesh_view(const fvh_host_mesh *m, fvh_mesh_view *o) {

@@ -1473,8 +1473,17 @@ fvh_status create_capacity(int dim, int64_t cells, int64_t faces, int64_t vertic
 }
 
 // Greedy face colouring on the host (faces in id order, the smallest colour
-// neither cell uses yet) for the colour schedule; deterministic.
+// neither cell uses yet) for the colour schedule; deterministic.  A failed host
+// allocation is reported as cudaErrorMemoryAllocation, not thrown.
+static cudaError_t setup_colours_host(workspace *w, const fvh_mesh_view &m);
 static cudaError_t setup_colours(workspace *w, const fvh_mesh_view &m) {
+  try {
+    return setup_colours_host(w, m);
+  } catch (const std::bad_alloc &) {
+    return cudaErrorMemoryAllocation;
+  }
+}
+static cudaError_t setup_colours_host(workspace *w, const fvh_mesh_view &m) {
   std::vector<int32_t> fc(2 * (size_t)m.num_faces);
   cudaError_t e = cudaMemcpy(fc.data(), m.face_cells, sizeof(int32_t) * fc.size(),
                              cudaMemcpyDeviceToHost);
@@ -1522,7 +1531,7 @@ fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) 
   if (e != cudaSuccess) {
     destroy(*out);
     *out = nullptr;
-    return FVH_ERR_CUDA;
+    return e == cudaErrorMemoryAllocation ? FVH_ERR_OUT_OF_MEMORY : FVH_ERR_CUDA;
   }
   return FVH_OK;
 }

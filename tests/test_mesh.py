@@ -110,3 +110,41 @@ def test_box_rejects_empty_and_inverted_extents(fvh):
         with pytest.raises(H.FvhError) as e:
             H.HostMesh.box(2, n, lo, hi)
         assert e.value.code == H.ERR_INVALID_ARGUMENT
+
+
+_OOM_CHILD = r'''
+import ctypes as C
+import resource
+import numpy as np
+import flecsale_gb300.hydro as H
+
+L = H.lib()
+resource.setrlimit(resource.RLIMIT_AS, (3 << 30, 3 << 30))
+h = C.c_void_p()
+lo, hi = np.zeros(3), np.ones(3)
+# 20000^2 quads: ~6.4 GB of vertex coordinates alone, far beyond the 3 GB limit
+rc_box = L.fvh_host_mesh_box(2, np.array([20000, 20000, 1], np.int32).ctypes.data_as(H._ip),
+                             H._dptr(lo), H._dptr(hi), 0.0, C.c_uint64(0), C.byref(h))
+print("box", rc_box, flush=True)
+# the library still works after the failures
+m = H.HostMesh.box(2, (8, 8), [0, 0], [1, 1])
+print("after", m.num_cells, flush=True)
+'''
+
+
+def test_host_allocation_failure_is_a_status_not_an_abort():
+    """A host allocation that fails inside a C entry point returns
+    FVH_ERR_OUT_OF_MEMORY instead of letting std::bad_alloc cross the C ABI
+    (which would terminate the caller); checked in a child process whose
+    address space is capped."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _OOM_CHILD], capture_output=True, text=True,
+                       timeout=300, cwd=root, env=dict(os.environ, PYTHONPATH=root,
+                                                       OMP_NUM_THREADS="2"))
+    assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
+    lines = dict(l.split(" ", 1) for l in r.stdout.splitlines())
+    assert int(lines["box"]) == H.ERR_OUT_OF_MEMORY
+    assert int(lines["after"]) == 64
