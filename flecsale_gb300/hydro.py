@@ -581,8 +581,11 @@ class Batch:
         t = np.zeros(n)
         codes = (C.c_int32 * n)()
         bad = (C.c_int64 * n)()
-        check(lib().fvh_batch_query(self._h, _dptr(t), codes, bad, stream_handle(stream)),
-              "fvh_batch_query")
+        rc = lib().fvh_batch_query(self._h, _dptr(t), codes, bad, stream_handle(stream))
+        # a failed problem (negative state, infinite dt) is reported in its own
+        # code; only argument and CUDA errors fail the query itself
+        if rc not in (OK, ERR_NEGATIVE_STATE, ERR_INFINITE_DT):
+            check(rc, "fvh_batch_query")
         return t, np.array(codes[:], np.int32), np.array(bad[:], np.int64)
 
     def set_shape(self, block: int, cells_per_thread: int, schedule: int = 0) -> None:
