@@ -76,3 +76,30 @@ def test_solver_and_batch_entry_points_reject_null_handles(fvh):
     assert L.fvh_solver_launches_per_run(None, 10) == 0
     assert L.fvh_debug_split(None, -1, None, None, None, None, None) == EI
     assert L.fvh_batch_step(None, 1, None) == EI
+
+
+def test_missing_library_fails_loudly_without_a_fallback(tmp_path):
+    """With the shared library absent and no CUDA compiler to build it, the
+    binding raises instead of falling back to any other implementation (in a
+    child process, so the library this session loaded stays untouched)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = f"""
+import shutil
+import flecsale_gb300._build as B
+import flecsale_gb300.hydro as H
+B.LIB = {str(tmp_path / 'absent' / 'libflecsale_gb300.so')!r}
+shutil.which = lambda name, *a, **k: None
+B._nvcc = lambda: (_ for _ in ()).throw(RuntimeError("nvcc not found: the CUDA toolkit is required"))
+try:
+    H.lib()
+except RuntimeError as e:
+    print("raised", e)
+else:
+    print("loaded")
+"""
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120,
+                       cwd=root, env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.startswith("raised") and "nvcc not found" in r.stdout, r.stdout
