@@ -48,7 +48,8 @@ typedef enum fvh_status {
   FVH_ERR_NEGATIVE_STATE = 4,     /* tasks.h:654-655 negative density or energy  */
   FVH_ERR_UNSUPPORTED = 5,        /* mesh cell shape / option not supported      */
   FVH_ERR_NO_DEVICE = 6,          /* no CUDA device visible                       */
-  FVH_ERR_OUT_OF_MEMORY = 7,
+  FVH_ERR_OUT_OF_MEMORY = 7,      /* a device or host allocation failed; no C++
+                                     exception ever crosses this ABI            */
   FVH_ERR_CAPACITY = 8            /* a request exceeds a fixed capacity           */
 } fvh_status;
 
@@ -347,7 +348,8 @@ fvh_status fvh_host_mesh_create(int32_t dim, int32_t num_vertices,
                                 const int32_t *cell_vertices,
                                 fvh_host_mesh **out);
 
-/* Structured-origin box mesh stored unstructured: n[0] x n[1] (x n[2]) cells on
+/* No reference counterpart (the reference reads its meshes from Exodus files):
+ * structured-origin box mesh stored unstructured: n[0] x n[1] (x n[2]) cells on
  * [lo, hi], vertex and cell ids lexicographic with x fastest.  Interior vertices
  * are moved by independent uniform offsets in [-jitter*h_k, +jitter*h_k] per axis
  * (SplitMix64 stream keyed by seed and vertex id); boundary vertices stay put. */
@@ -380,7 +382,8 @@ fvh_status fvh_host_state_from_dvp(int32_t dim, int32_t n, double gamma, double 
                                    const double *density, const double *velocity,
                                    const double *pressure, double *host_planes);
 
-/* Concatenate meshes of one dimension into one block-diagonal mesh: cells,
+/* No reference counterpart (used by the batched form).  Concatenate meshes of
+ * one dimension into one block-diagonal mesh: cells,
  * faces and vertices of mesh k follow those of meshes 0..k-1, with all indices
  * shifted; no connectivity is added between meshes. */
 fvh_status fvh_host_mesh_concat(int32_t n, const fvh_host_mesh *const *meshes,
@@ -419,6 +422,9 @@ fvh_status fvh_host_initial_state(int32_t kind, const fvh_host_mesh *m,
 /* ------------------------------------------------------------------------- */
 /* Device memory helpers (setup only, never called inside a step)             */
 /* ------------------------------------------------------------------------- */
+/* In the reference the FleCSI data model owns all field storage (fields
+ * registered at apps/hydro/driver.h:33-158); these helpers are the optional
+ * owner for callers that do not manage device memory themselves. */
 typedef struct fvh_device_mesh fvh_device_mesh;
 
 /* Copy a host mesh to device memory. */
@@ -442,7 +448,8 @@ fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim,
                               int32_t num_cells, double *host_planes,
                               fvh_stream_t stream);
 
-/* End-to-end call for callers that hold the state in host memory: upload the
+/* No reference counterpart.  End-to-end call for callers that hold the state
+ * in host memory: upload the
  * state, advance nsteps time steps, download it, then synchronise.  Solution
  * time in/out through *soln_time.  With pinned host planes (cudaHostAlloc /
  * cudaHostRegister) and the mixed form the kernels read the state from and
