@@ -313,6 +313,101 @@ fvh_status fvh_dump_write(const char *path, const fvh_host_mesh *m, const double
   return ok ? FVH_OK : FVH_ERR_INVALID_ARGUMENT;
 }
 
+fvh_status fvh_dump_read(const char *path, int32_t dim, int32_t num_cells, double gamma,
+                         double cv, double *host_planes, double *soln_time,
+                         int64_t *iterations) {
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!path || (dim != 2 && dim != 3) || num_cells <= 0 || !host_planes || !(gamma > 1) ||
+        !(cv > 0))
+      return FVH_ERR_INVALID_ARGUMENT;
+    std::FILE *f = std::fopen(path, "r");
+    if (!f) return FVH_ERR_INVALID_ARGUMENT;
+    std::string line;
+    auto next_line = [&]() -> bool {
+      line.clear();
+      int ch;
+      while ((ch = std::fgetc(f)) != EOF && ch != '\n') line.push_back((char)ch);
+      return ch != EOF || !line.empty();
+    };
+    auto after = [&](const char *prefix) -> const char * {
+      const size_t n = std::strlen(prefix);
+      return line.compare(0, n, prefix) == 0 ? line.c_str() + n : nullptr;
+    };
+    // header: "# Solution time: t", "# Number iterations: n", "# BEGIN CELLS",
+    // "# Total number: N", then the column-name line (tasks.h:805-820)
+    double t = 0;
+    long long iters = 0;
+    bool have_t = false, have_n = false, in_cells = false;
+    int64_t total = -1;
+    fvh_status st = FVH_OK;
+    while (st == FVH_OK && next_line()) {
+      const char *v = nullptr;
+      char *end = nullptr;
+      if ((v = after("# Solution time:"))) {
+        t = std::strtod(v, &end);
+        have_t = end != v;
+      } else if ((v = after("# Number iterations:"))) {
+        iters = std::strtoll(v, &end, 10);
+        have_n = end != v;
+      } else if (after("# BEGIN CELLS")) {
+        in_cells = true;
+      } else if (in_cells && (v = after("# Total number:"))) {
+        total = std::strtoll(v, &end, 10);
+        if (end == v || total != num_cells) st = FVH_ERR_INVALID_ARGUMENT;
+        if (st == FVH_OK && !next_line()) st = FVH_ERR_INVALID_ARGUMENT;  // column names
+        break;
+      }
+    }
+    if (st == FVH_OK && (!have_t || !have_n || total != num_cells)) st = FVH_ERR_INVALID_ARGUMENT;
+    // rows: local_id global_id centroid[dim] density internal_energy pressure velocity[dim]
+    const size_t nc = (size_t)num_cells;
+    double *d = host_planes, *e = host_planes + (size_t)(1 + dim) * nc, *pr = e + nc, *T = pr + nc,
+           *a = T + nc;
+    std::vector<char> seen(nc, 0);
+    for (size_t row = 0; st == FVH_OK && row < nc; ++row) {
+      if (!next_line()) {
+        st = FVH_ERR_INVALID_ARGUMENT;
+        break;
+      }
+      const int nv = 2 + dim + 3 + dim;
+      double x[2 + 3 + 3 + 3];
+      const char *q = line.c_str();
+      for (int k = 0; k < nv && st == FVH_OK; ++k) {
+        char *end = nullptr;
+        x[k] = std::strtod(q, &end);
+        if (end == q || !std::isfinite(x[k])) st = FVH_ERR_INVALID_ARGUMENT;
+        q = end;
+      }
+      while (st == FVH_OK && *q != '\0') {  // nothing but blanks after the last column
+        if (!std::isspace((unsigned char)*q)) st = FVH_ERR_INVALID_ARGUMENT;
+        ++q;
+      }
+      if (st != FVH_OK) break;
+      const double id = x[0];
+      if (!(id >= 0 && id < (double)nc) || id != std::floor(id) || seen[(size_t)id]) {
+        st = FVH_ERR_INVALID_ARGUMENT;
+        break;
+      }
+      const size_t c = (size_t)id;
+      seen[c] = 1;
+      const double *w = x + 2 + dim;  // density internal_energy pressure velocity...
+      d[c] = w[0];
+      e[c] = w[1];
+      pr[c] = w[2];
+      for (int k = 0; k < dim; ++k) host_planes[(size_t)(1 + k) * nc + c] = w[3 + k];
+      // closure from the internal energy (update_state_from_energy, euler_eqns.h:359-375)
+      T[c] = w[1] / cv;
+      a[c] = std::sqrt(gamma * (gamma - 1.0) * w[1]);
+    }
+    if (st == FVH_OK && (!next_line() || !after("# END CELLS"))) st = FVH_ERR_INVALID_ARGUMENT;
+    std::fclose(f);
+    if (st != FVH_OK) return st;
+    if (soln_time) *soln_time = t;
+    if (iterations) *iterations = (int64_t)iters;
+    return FVH_OK;
+  });
+}
+
 fvh_status fvh_host_state_from_dvp(int32_t dim, int32_t n, double gamma, double cv,
                                    const double *density, const double *velocity,
                                    const double *pressure, double *host_planes) {

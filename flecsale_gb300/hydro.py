@@ -622,6 +622,8 @@ def _declare_io(L: C.CDLL) -> None:
         ("fvh_dump_write", C.c_int, [C.c_char_p, vp, _dp, C.c_double, C.c_int64]),
         ("fvh_host_state_from_dvp", C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double,
                                                _dp, _dp, _dp, _dp]),
+        ("fvh_dump_read", C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                    _dp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ]:
         fn = getattr(L, name)
         fn.restype, fn.argtypes = res, args
@@ -643,6 +645,19 @@ def write_dump(path: str, mesh: HostMesh, planes: np.ndarray, soln_time: float,
                            "write_dump")
     check(lib().fvh_dump_write(path.encode(), mesh._h, _dptr(planes), soln_time, iterations),
           "fvh_dump_write")
+
+
+def read_dump(path: str, dim: int, num_cells: int, gamma: float = 1.4,
+              cv: float = 1.0) -> tuple:
+    """(state planes, solution time, iterations) from a regression dump
+    (fvh_dump_read): resumes a run from the text the reference's dump task
+    and write_dump produce."""
+    _declare_io(lib())
+    out = np.empty((5 + dim, num_cells), np.float64)
+    t, n = C.c_double(), C.c_int64()
+    check(lib().fvh_dump_read(path.encode(), dim, num_cells, gamma, cv, _dptr(out), C.byref(t),
+                              C.byref(n)), f"read_dump({path})")
+    return out, t.value, n.value
 
 
 def state_from_dvp(dim: int, density, velocity, pressure, gamma: float = 1.4,

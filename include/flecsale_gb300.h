@@ -374,6 +374,19 @@ fvh_status fvh_dump_write(const char *path, const fvh_host_mesh *m,
                           const double *host_planes, double soln_time,
                           int64_t iterations);
 
+/* Read a regression dump (the format above and of tasks.h:771-849) back into
+ * host state planes (d, v[0..dim), e, p, T, a) of num_cells cells, by local_id:
+ * density, internal energy, pressure and velocity as printed (15 significant
+ * digits), T = e / cv and a = sqrt(gamma (gamma - 1) e) as
+ * update_state_from_energy closes them (euler_eqns.h:359-375).  The header's
+ * solution time and iteration count go to *soln_time and *iterations (either
+ * may be null).  A dump whose cell count differs, or that is malformed, gives
+ * FVH_ERR_INVALID_ARGUMENT.  No reference counterpart (the reference only
+ * writes dumps); it lets a run resume from one. */
+fvh_status fvh_dump_read(const char *path, int32_t dim, int32_t num_cells, double gamma,
+                         double cv, double *host_planes, double *soln_time,
+                         int64_t *iterations);
+
 /* EOS closure of caller-provided density, velocity planes [dim][n] and
  * pressure (update_state_from_pressure, euler_eqns.h:333-350) into state
  * planes d, v..., e, p, T, a: the second half of initial_conditions

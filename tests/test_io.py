@@ -175,3 +175,68 @@ def test_exodus_reader_survives_malformed_files(tmp_path):
                        env=dict(os.environ, PYTHONPATH=root))
     assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
     assert "refused" in r.stdout
+
+
+def test_read_dump_of_the_reference_golden(tmp_path):
+    """The reference's own 2D regression dump reads back into the printed
+    values (bitwise: the text holds them exactly), with its header time and
+    iteration count."""
+    path = str(tmp_path / "golden.txt")
+    with open(path, "w") as f:
+        f.write("\n".join(golden_2d_text()) + "\n")
+    z = np.load(os.path.join(U.GOLDEN, "shock_box_2d_32x32.npz"))
+    s, t, n = H.read_dump(path, 2, len(z["cells"]))
+    assert t == float(z["soln_time"]) and n == int(z["iterations"])
+    assert np.array_equal(U.dump_columns(s, 2), z["cells"])
+    e = s[3]
+    assert np.array_equal(s[5], e) and np.array_equal(s[6], np.sqrt(1.4 * (1.4 - 1.0) * e))
+
+
+def test_restart_from_a_dump_continues_the_run(tmp_path, oracle_lib):
+    """20 oracle steps in one go and 10 + dump + read + 10 agree to the dump's
+    print precision (15 significant digits, grown by 10 steps)."""
+    mesh, _ = U.golden_2d()
+    p = H.make_params(2)
+    straight = H.initial_state("shock_box", mesh, p)
+    st, t20, _ = U.oracle_run(oracle_lib, mesh, straight, p, 20)
+    assert st == 0
+    half = H.initial_state("shock_box", mesh, p)
+    st, t10, n10 = U.oracle_run(oracle_lib, mesh, half, p, 10)
+    path = str(tmp_path / "restart.txt")
+    H.write_dump(path, mesh, half, t10, n10)
+    resumed, t_read, n_read = H.read_dump(path, 2, mesh.num_cells, p.gamma, p.cv)
+    assert n_read == 10 and abs(t_read - t10) <= 1e-15 * t10
+    assert np.abs(resumed - half).max() <= 1e-14 * np.abs(half).max()
+    st, t_end, _ = U.oracle_run(oracle_lib, mesh, resumed, p, 10, t=t_read)
+    assert st == 0 and abs(t_end - t20) <= 1e-13
+    assert np.abs(resumed - straight).max() <= 1e-12
+
+
+def test_read_dump_refuses_malformed_dumps(tmp_path):
+    mesh = H.HostMesh.box(3, (3, 2, 2), [0, 0, 0], [1, 1, 1], 0.1, 2)
+    p = H.make_params(3)
+    s = H.initial_state("inner_cube", mesh, p)
+    good = str(tmp_path / "good.txt")
+    H.write_dump(good, mesh, s, 0.25, 7)
+    back, t, n = H.read_dump(good, 3, mesh.num_cells)
+    assert (t, n) == (0.25, 7) and np.allclose(back, s, rtol=1e-14, atol=0)
+    text = open(good).read().splitlines()
+    first_row = text.index("# BEGIN CELLS") + 3
+    cases = {
+        "wrong_count": (good, 2, mesh.num_cells + 1),
+        "wrong_dim": (good, 2, mesh.num_cells),
+        "truncated": ("\n".join(text[:first_row + 4]), 3, mesh.num_cells),
+        "duplicate_id": ("\n".join(text[:first_row] + [text[first_row]] * 2 + text[first_row + 2:]),
+                         3, mesh.num_cells),
+        "bad_number": ("\n".join(text[:first_row] + [text[first_row].replace("e", "x", 1)]
+                                 + text[first_row + 1:]), 3, mesh.num_cells),
+        "no_header": ("\n".join(text[2:]), 3, mesh.num_cells),
+        "empty": ("", 3, mesh.num_cells),
+    }
+    for name, (content, dim, nc) in cases.items():
+        path = content if content == good else str(tmp_path / f"{name}.txt")
+        if content != good:
+            with open(path, "w") as f:
+                f.write(content)
+        with pytest.raises(H.FvhError):
+            H.read_dump(path, dim, nc)
