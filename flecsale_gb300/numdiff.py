@@ -1,19 +1,25 @@
 """Line-by-line numeric diff of two text dumps, with the comparison semantics of
 the reference's regression tool (tools/numdiff.py: softEquiv, :70-96; run,
-:181-217): columns are split on whitespace; numeric columns must agree within
-the relative tolerance (if > 0) and the absolute tolerance (if > 0); other
-columns must match exactly when check_text is set; the files must have the
-same number of lines.  The reference's regression tests use
+:181-217): columns are split on commas, semicolons and whitespace (:23);
+numeric columns must agree within the relative tolerance (if > 0) and the
+absolute tolerance (if > 0); other columns must match exactly when check_text
+is set; the comparison ends at the first empty line of the expected file, and
+the tested file must end there too.  The reference's regression tests use
 `--check-text --absolute 1e-14` (cmake/regression.cmake:19).
+
+Command line, with the reference tool's options and exit status (:222-266):
+    python -m flecsale_gb300.numdiff [-c] [-a ABS] [-r REL] [-t TOL] [-q] [-v] expected actual
 """
 from __future__ import annotations
 
+import argparse
 import math
 import re
+import sys
 from dataclasses import dataclass, field
-from typing import List
+from typing import List, Optional
 
-_SPLIT = re.compile(r"\s+")
+_SPLIT = re.compile(r",|\s+|;")
 
 
 @dataclass
@@ -53,10 +59,11 @@ def compare_lines(expected: List[str], actual: List[str], rel_tol: float = -1.0,
     for i in range(n):
         e = expected[i].rstrip() if i < len(expected) else ""
         a = actual[i].rstrip() if i < len(actual) else ""
-        if e == "" and a != "":
-            rep.fail("tested file ended too late")
+        if e == "":
+            if a != "":
+                rep.fail("tested file ended too late")
             break
-        if a == "" and e != "":
+        if a == "":
             rep.fail("tested file ended too early")
             break
         ec, ac = _split(e), _split(a)
@@ -83,3 +90,34 @@ def compare_lines(expected: List[str], actual: List[str], rel_tol: float = -1.0,
 def compare_files(expected_path: str, actual_path: str, **kw) -> Report:
     with open(expected_path) as fe, open(actual_path) as fa:
         return compare_lines(fe.read().splitlines(), fa.read().splitlines(), **kw)
+
+
+def main(argv: Optional[List[str]] = None) -> int:
+    """The reference tool's command line: exit status 0 and SUCCESS when the
+    files agree, 1 and FAILURE (after one ">>>> reason" line per failure, at
+    most 20) otherwise.  Without -r and -a both tolerances are -t (1e-15)."""
+    ap = argparse.ArgumentParser(description="numeric diff of two text files")
+    ap.add_argument("-q", "--quiet", action="store_true")
+    ap.add_argument("-v", "--verbose", action="count", default=0)
+    ap.add_argument("-c", "--check-text", action="store_true")
+    ap.add_argument("-t", "--tolerance", type=float, default=1e-15)
+    ap.add_argument("-r", "--relative", type=float, default=-1.0)
+    ap.add_argument("-a", "--absolute", type=float, default=-1.0)
+    ap.add_argument("files", nargs="*")
+    args = ap.parse_args(argv)
+    if len(args.files) != 2:
+        ap.print_help()
+        return 1
+    rel, abs_ = args.relative, args.absolute
+    if rel < 0 and abs_ < 0:
+        rel = abs_ = args.tolerance
+    rep = compare_files(args.files[0], args.files[1], rel_tol=rel, abs_tol=abs_,
+                        check_text=args.check_text)
+    for msg in rep.failures:
+        print(">>>> " + msg)
+    print("SUCCESS" if rep.ok else "FAILURE")
+    return 0 if rep.ok else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main())

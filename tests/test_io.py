@@ -240,3 +240,46 @@ def test_read_dump_refuses_malformed_dumps(tmp_path):
                 f.write(content)
         with pytest.raises(H.FvhError):
             H.read_dump(path, dim, nc)
+
+
+def test_numdiff_command_line_matches_the_reference_tool(tmp_path):
+    """`python -m flecsale_gb300.numdiff` takes the reference tool's options and
+    gives its exit status on passing and failing pairs (and, where the
+    reference checkout exists, the same status as tools/numdiff.py itself)."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    golden = golden_2d_text()
+    base = str(tmp_path / "a.txt")
+    with open(base, "w") as f:
+        f.write("\n".join(golden) + "\n")
+    row = golden.index("# BEGIN CELLS") + 3
+
+    def variant(name, lines):
+        path = str(tmp_path / name)
+        with open(path, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        return path
+
+    cols = golden[row].split()
+    near = cols[:4] + [f"{float(cols[4]) + 5e-15:.14e}"] + cols[5:]
+    far = cols[:4] + [f"{float(cols[4]) + 5e-13:.14e}"] + cols[5:]
+    cases = [
+        (["--check-text", "--verbose", "--absolute", "1e-14"], base, 0),
+        (["-c", "-a", "1e-14"], variant("near.txt", golden[:row] + [" ".join(near)] + golden[row + 1:]), 0),
+        (["-c", "-a", "1e-14"], variant("far.txt", golden[:row] + [" ".join(far)] + golden[row + 1:]), 1),
+        (["-a", "1e-12"], variant("far2.txt", golden[:row] + [" ".join(far)] + golden[row + 1:]), 0),
+        (["-c", "-a", "1e-14"], variant("text.txt", [golden[0].replace("Solution", "solution")] + golden[1:]), 1),
+        ([], variant("text2.txt", [golden[0].replace("Solution", "solution")] + golden[1:]), 0),
+        (["-c", "-a", "1e-14"], variant("short.txt", golden[:-5]), 1),
+        (["-c", "-r", "1e-3"], variant("rel.txt", golden[:row] + [" ".join(far)] + golden[row + 1:]), 0),
+    ]
+    ref_tool = os.path.join(U.REFERENCE, "tools", "numdiff.py")
+    for opts, other, want in cases:
+        r = subprocess.run([sys.executable, "-m", "flecsale_gb300.numdiff", *opts, base, other],
+                           capture_output=True, text=True, cwd=root, env=dict(os.environ, PYTHONPATH=root))
+        assert r.returncode == want, (opts, other, r.stdout[-500:])
+        assert r.stdout.rstrip().endswith("SUCCESS" if want == 0 else "FAILURE")
+        if os.path.exists(ref_tool):
+            q = subprocess.run([sys.executable, ref_tool, *opts, base, other], capture_output=True, text=True)
+            assert q.returncode == want, (opts, other, q.stdout[-500:])
