@@ -21,6 +21,12 @@
  *  - Results are deterministic: no floating-point atomics are used anywhere; the
  *    face-to-cell accumulation is a cell-centric gather in the cell's face order.
  *  - dim is 2 or 3.  Index arrays are int32.
+ *  - Threads: a handle (fvh_solver, fvh_batch, fvh_input, meshes and states)
+ *    is used by one thread at a time, since a solver or batch keeps per-stream
+ *    CUDA graphs and pinned scalars; distinct handles may be used concurrently
+ *    from different threads on different streams.  The task entry points keep
+ *    no state between calls (fvh_evaluate_time_step_noalloc excepted: its
+ *    calls share one scratch array, see there).
  */
 #ifndef FLECSALE_GB300_H
 #define FLECSALE_GB300_H
