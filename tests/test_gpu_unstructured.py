@@ -11,46 +11,6 @@ from tests import _util as U
 pytestmark = pytest.mark.gpu
 
 
-def _tri_mesh(n=(30, 22), split_every=1, seed=3):
-    """A jittered quad box with every split_every-th quad cut into two
-    triangles (alternating diagonals)."""
-    box = H.HostMesh.box(2, n, [0, 0], [1, 1], 0.2, seed)
-    a = box.arrays()
-    coords = a["vertex_coord"].T.copy()
-    quads = a["cell_vertices"].reshape(-1, 4)
-    cells, offs = [], [0]
-    for k, q in enumerate(quads):
-        if k % split_every == 0:
-            t = ((q[0], q[1], q[2]), (q[0], q[2], q[3])) if k % 2 else \
-                ((q[0], q[1], q[3]), (q[1], q[2], q[3]))
-            for tri in t:
-                cells += tri
-                offs.append(len(cells))
-        else:
-            cells += list(q)
-            offs.append(len(cells))
-    return H.HostMesh.from_cells(2, coords, np.array(offs, np.int32), np.array(cells, np.int32))
-
-
-def _tet_mesh(n=(6, 5, 5), seed=2):
-    """A jittered hex box with each hex cut into 6 tetrahedra around its main
-    diagonal, each ordered to positive volume."""
-    box = H.HostMesh.box(3, n, [0, 0, 0], [1, 1, 1], 0.15, seed)
-    a = box.arrays()
-    x = a["vertex_coord"].T.copy()
-    hexes = a["cell_vertices"].reshape(-1, 8)
-    cells = []
-    for h in hexes:
-        for t in ((0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6)):
-            v = [h[i] for i in t]
-            d = np.linalg.det(np.stack([x[v[1]] - x[v[0]], x[v[2]] - x[v[0]], x[v[3]] - x[v[0]]]))
-            if d < 0:
-                v[1], v[2] = v[2], v[1]
-            cells += v
-    return H.HostMesh.from_cells(3, x, np.arange(0, len(cells) + 1, 4, dtype=np.int32),
-                                 np.array(cells, np.int32))
-
-
 def _run(mesh, p, state, nsteps):
     dm, ds = H.DeviceMesh(mesh), H.DeviceState(mesh.dim, mesh.num_cells)
     s = H.Solver(dm, p)
@@ -63,9 +23,9 @@ def _run(mesh, p, state, nsteps):
 
 
 MESHES = {
-    "triangles": lambda: _tri_mesh(),
-    "quad_tri_mix": lambda: _tri_mesh(split_every=3),
-    "tetrahedra": lambda: _tet_mesh(),
+    "triangles": lambda: U.tri_mesh(),
+    "quad_tri_mix": lambda: U.tri_mesh(split_every=3),
+    "tetrahedra": lambda: U.tet_mesh(),
 }
 
 

@@ -9,14 +9,13 @@ import pytest
 import flecsale_gb300.hydro as H
 from tests import _util as U
 from tests.test_exact_riemann import GAMMA, SOD_L, SOD_R, exact_riemann
-from tests.test_gpu_unstructured import _tet_mesh, _tri_mesh
 
 MESHES = {
     "quads_jittered": lambda: H.HostMesh.box(2, (24, 20), [0, 0], [1, 1], 0.2, 5),
-    "quad_tri_mix": lambda: _tri_mesh((20, 16), split_every=3),
-    "triangles": lambda: _tri_mesh((16, 14)),
+    "quad_tri_mix": lambda: U.tri_mesh((20, 16), split_every=3),
+    "triangles": lambda: U.tri_mesh((16, 14)),
     "hexes_jittered": lambda: H.HostMesh.box(3, (8, 7, 6), [0, 0, 0], [1, 1, 1], 0.15, 6),
-    "tetrahedra": lambda: _tet_mesh((4, 4, 3)),
+    "tetrahedra": lambda: U.tet_mesh((4, 4, 3)),
 }
 
 
