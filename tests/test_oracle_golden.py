@@ -109,3 +109,30 @@ def test_product_closure_matches_oracle(fvh, oracle_lib):
     d, pr = np.ascontiguousarray(s[0]), np.ascontiguousarray(s[4])
     oracle_lib.oracle_state_from_pressure(nc, 1.67, 0.7, *(x.ctypes.data_as(dp) for x in (d, pr, e, T, a)))
     assert np.array_equal(e, s[3]) and np.array_equal(T, s[5]) and np.array_equal(a, s[6])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_threads_do_not_change_the_bits(fvh, oracle_lib, dim):
+    """The CPU baseline times the oracle on one thread and on all host
+    threads; both compute the same bits (cells are independent within a task
+    and the dt reduction is a minimum), so the two timings measure the same
+    work."""
+    if dim == 2:
+        mesh = fvh.HostMesh.box(2, (60, 50), [0, 0], [1, 1], 0.2, 3)
+        p = fvh.make_params(2, flux="hllc", cfl=0.4, boundary="outflow")
+        kind = "four_quadrant"
+    else:
+        mesh = fvh.HostMesh.box(3, (12, 10, 9), [0, 0, 0], [1, 1, 1], 0.15, 4)
+        p = fvh.make_params(3, flux="rusanov", cfl=0.3)
+        kind = "inner_cube"
+    out = []
+    try:
+        for threads in (1, 0):
+            oracle_lib.oracle_set_threads(threads)
+            s = fvh.initial_state(kind, mesh, p)
+            st, t, _ = U.oracle_run(oracle_lib, mesh, s, p, 8)
+            assert st == 0
+            out.append((s, t))
+    finally:
+        oracle_lib.oracle_set_threads(0)
+    assert out[0][1] == out[1][1] and np.array_equal(out[0][0], out[1][0])
