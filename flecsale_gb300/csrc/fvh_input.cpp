@@ -4,6 +4,7 @@
 // the box mesh table of apps/hydro/3d/shock_box_3d.lua.  Evaluated with the
 // Lua-subset interpreter of fvh_lua.cpp.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <new>
