@@ -582,7 +582,12 @@ fvh_status fvh_batch_step(fvh_batch *b, int32_t nsteps, fvh_stream_t stream) {
     e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return from_cuda(e);
-    it = b->graphs.emplace(nsteps, ex).first;
+    try {  // no exception crosses the C ABI
+      it = b->graphs.emplace(nsteps, ex).first;
+    } catch (const std::bad_alloc &) {
+      cudaGraphExecDestroy(ex);
+      return FVH_ERR_OUT_OF_MEMORY;
+    }
   }
   return from_cuda(cudaGraphLaunch(it->second, st));
 }
