@@ -56,6 +56,18 @@ def build_problem(n_side: int = N_SIDE):
     return H, mesh, p64, p32, state0
 
 
+def conservation_totals(mesh, state) -> dict:
+    """Mass, momentum and total energy of a state: FP64 sums over cells of the
+    conserved variables (rho, rho v, rho (e + |v|^2 / 2)) times the cell
+    volumes."""
+    D = mesh.dim
+    vol = mesh.arrays()["cell_volume"]
+    d, v, e = state[0], state[1:1 + D], state[1 + D]
+    return {"mass": float(np.dot(d, vol)),
+            "momentum": [float(np.dot(d * v[k], vol)) for k in range(D)],
+            "energy": float(np.dot(d * (e + 0.5 * (v * v).sum(axis=0)), vol))}
+
+
 # ---------------------------------------------------------------------------
 # algorithmic bytes per launch (each array a kernel must touch, moved once)
 # ---------------------------------------------------------------------------
@@ -590,6 +602,11 @@ def run_ours(args):
                      "l1_total_energy_mixed_vs_fp64": l1(E(m), E(f)),
                      "linf_density_mixed_vs_fp64": float(np.abs(m[0] - f[0]).max()),
                      "linf_total_energy_mixed_vs_fp64": float(np.abs(E(m) - E(f)).max())},
+        "conservation": {"note": "FP64 totals; outflow boundaries, so they change by the "
+                                 "boundary fluxes",
+                         "initial": conservation_totals(mesh, state0),
+                         "fp64": conservation_totals(mesh, f),
+                         "mixed": conservation_totals(mesh, m)},
     }
     if not args.no_batch:
         line["batched"] = run_batched(torch, stream, min(args.steps, 50), args.warmup)

@@ -122,3 +122,27 @@ def test_write_dump_refuses_short_planes(tmp_path):
     with pytest.raises(ValueError):
         H.write_dump(str(tmp_path / "d.txt"), mesh, np.zeros((7, mesh.num_cells - 1)), 0.0, 0)
     assert not (tmp_path / "d.txt").exists()
+
+
+def test_bench_conservation_totals(oracle_lib):
+    """The bench's conservation totals: exact for a uniform state, and mass
+    and energy kept to rounding by an oracle run between walls."""
+    import bench
+    from tests import _util as U
+    mesh = H.HostMesh.box(2, (20, 16), [0, 0], [2, 1], 0.2, 5)
+    p = H.make_params(2, flux="hllc", cfl=0.4)
+    n = mesh.num_cells
+    s = H.state_from_dvp(2, np.full(n, 2.0), np.stack([np.full(n, 0.5), np.full(n, -1.0)]),
+                         np.full(n, 0.8), p.gamma, p.cv)
+    tot = bench.conservation_totals(mesh, s)
+    e = 0.8 / (2.0 * 0.4)
+    assert abs(tot["mass"] - 4.0) <= 1e-13
+    assert np.allclose(tot["momentum"], [2.0, -4.0], rtol=1e-13)
+    assert abs(tot["energy"] - 4.0 * (e + 0.5 * 1.25)) <= 1e-12
+    s = H.initial_state("four_quadrant", mesh, p)
+    t0 = bench.conservation_totals(mesh, s)
+    st, _, _ = U.oracle_run(oracle_lib, mesh, s, p, 10)
+    t1 = bench.conservation_totals(mesh, s)
+    assert st == 0
+    assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * t0["mass"]
+    assert abs(t1["energy"] - t0["energy"]) <= 1e-13 * t0["energy"]
