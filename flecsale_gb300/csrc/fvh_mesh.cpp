@@ -185,12 +185,17 @@ fvh_status build_topology_and_geometry(fvh_host_mesh &m) {
   const int dim = m.dim, nc = m.nc, nv = m.nv;
   // vertex -> cells, ascending cell id
   std::vector<int32_t> vc_off(nv + 1, 0), vcl;
-  for (int c = 0; c < nc; ++c)
+  for (int c = 0; c < nc; ++c) {
     for (int k = m.cv_off[c]; k < m.cv_off[c + 1]; ++k) {
       const int v = m.cv[k];
       if (v < 0 || v >= nv) return FVH_ERR_INVALID_ARGUMENT;
+      // a vertex listed twice makes a degenerate face that would match a
+      // neighbour sharing that vertex
+      for (int j = m.cv_off[c]; j < k; ++j)
+        if (m.cv[j] == v) return FVH_ERR_INVALID_ARGUMENT;
       vc_off[v + 1]++;
     }
+  }
   for (int v = 0; v < nv; ++v) vc_off[v + 1] += vc_off[v];
   vcl.resize(vc_off[nv]);
   {
@@ -229,6 +234,10 @@ fvh_status build_topology_and_geometry(fvh_host_mesh &m) {
       if (count > 1) bad = 1;
       lf_nbr[lf_off[c] + k] = found;
     }
+    // two faces of one cell shared with the same neighbour: not supported
+    for (int64_t q = lf_off[c]; q < lf_off[c + 1]; ++q)
+      for (int64_t r = lf_off[c]; r < q; ++r)
+        if (lf_nbr[q] >= 0 && lf_nbr[q] == lf_nbr[r]) bad = 1;
   }
   if (bad) return FVH_ERR_UNSUPPORTED;  // non-manifold face
 
@@ -271,6 +280,22 @@ fvh_status build_topology_and_geometry(fvh_host_mesh &m) {
       const int f = lf_face[q];
       m.cf[q] = (m.face_cells[2 * (size_t)f] == c) ? f : ~f;
     }
+
+  // every interior face is listed by its second cell too (as ~f), exactly once:
+  // otherwise its flux would leave one cell and enter none
+  {
+    std::vector<int32_t> second(nf, -1);
+    for (int c = 0; c < nc && !bad; ++c)
+      for (int64_t q = lf_off[c]; q < lf_off[c + 1]; ++q)
+        if (m.cf[q] < 0) {
+          const int f = ~m.cf[q];
+          if (second[f] >= 0 || m.face_cells[2 * (size_t)f + 1] != c) bad = 1;
+          second[f] = c;
+        }
+    for (int f = 0; f < nf && !bad; ++f)
+      if ((m.face_cells[2 * (size_t)f + 1] >= 0) != (second[f] >= 0)) bad = 1;
+    if (bad) return FVH_ERR_UNSUPPORTED;
+  }
 
   // face -> vertices (creator's orientation)
   std::vector<int> fnv(nf, 0);
@@ -369,6 +394,22 @@ fvh_status build_topology_and_geometry(fvh_host_mesh &m) {
   }
   for (int c = 0; c < nc; ++c)
     if (!(m.cvol[c] > 0)) return FVH_ERR_INVALID_ARGUMENT;  // inverted cell
+  for (int f = 0; f < nf; ++f)
+    if (!(m.fa[f] > 0)) return FVH_ERR_INVALID_ARGUMENT;    // face of zero extent
+  // every cell is closed: the sum of its outward area vectors vanishes (to
+  // rounding), so a uniform state is a steady state of the update
+  for (int c = 0; c < nc; ++c) {
+    double sum[3] = {0, 0, 0}, area = 0;
+    for (int64_t q = m.cf_off[c]; q < m.cf_off[c + 1]; ++q) {
+      const int32_t e = m.cf[q];
+      const int f = e >= 0 ? e : ~e;
+      const double sgn = e >= 0 ? 1.0 : -1.0;
+      for (int d = 0; d < dim; ++d) sum[d] += sgn * m.fa[f] * m.fn[d][f];
+      area += m.fa[f];
+    }
+    const double gap = std::sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]);
+    if (!(gap <= 1e-10 * area)) return FVH_ERR_INVALID_ARGUMENT;
+  }
   return FVH_OK;
 }
 

@@ -148,3 +148,30 @@ def test_host_allocation_failure_is_a_status_not_an_abort():
     lines = dict(l.split(" ", 1) for l in r.stdout.splitlines())
     assert int(lines["box"]) == H.ERR_OUT_OF_MEMORY
     assert int(lines["after"]) == 64
+
+
+def _polys(coords, cells):
+    off = np.cumsum([0] + [len(c) for c in cells]).astype(np.int32)
+    return H.HostMesh.from_cells(2, np.asarray(coords, float), off,
+                                 np.concatenate(cells).astype(np.int32))
+
+
+def test_invalid_polygon_meshes_are_refused(fvh):
+    """Meshes whose faces would not close a cell are refused instead of
+    giving a non-conservative update: a vertex listed twice in a cell, two
+    cells sharing two edges, a cell edge lying across another cell (either
+    cell order) and an edge of zero length."""
+    sq = [[0, 0], [1, 0], [1, 1], [0, 1]]
+    ok = _polys(sq + [[2, 0]], [[0, 1, 2, 3], [1, 4, 2]])
+    assert ok.num_cells == 2 and ok.num_faces == 6
+    cases = {
+        "repeated_vertex": (sq + [[2, 0]], [[0, 1, 2, 3], [1, 4, 2, 2]]),
+        "two_shared_edges": ([[0, 0], [2, 0], [1, 1], [2, 2], [0, 2]], [[0, 1, 2, 3, 4], [1, 3, 2]]),
+        "edge_across_a_cell": (sq + [[0, 2]], [[0, 1, 2, 3], [0, 2, 4]]),
+        "edge_across_a_cell_first": (sq + [[0, 2]], [[0, 2, 4], [0, 1, 2, 3]]),
+        "zero_length_edge": (sq + [[1, 0]], [[0, 4, 1, 2, 3]]),
+    }
+    for name, (coords, cells) in cases.items():
+        with pytest.raises(H.FvhError) as e:
+            _polys(coords, cells)
+        assert e.value.code in (H.ERR_INVALID_ARGUMENT, H.ERR_UNSUPPORTED), name
