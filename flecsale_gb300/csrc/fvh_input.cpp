@@ -137,61 +137,75 @@ fvh_status fvh_input_params(const fvh_input *in, fvh_params *p, int64_t *max_ste
 }
 
 fvh_status fvh_input_mesh(const fvh_input *in, fvh_host_mesh **out) {
-  if (!in || !out) return FVH_ERR_INVALID_ARGUMENT;
-  *out = nullptr;
-  const Value mesh = at(in, "hydro.mesh");
-  if (mesh.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
-  const Value type = fvh::lua::lookup(mesh, "type");
-  if (type.kind != Value::STRING || type.s != "box") return FVH_ERR_UNSUPPORTED;
-  const Value dims = fvh::lua::lookup(mesh, "dimensions");
-  if (dims.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
-  const int dim = (int)dims.t->array.size();
-  if (dim != 2 && dim != 3) return FVH_ERR_INVALID_ARGUMENT;
-  int32_t n[3];
-  double lo[3], hi[3];
-  for (int k = 0; k < dim; ++k) {
-    double v;
-    const std::string idx = "[" + std::to_string(k + 1) + "]";
-    if (!as_number(dims.t->array[k], &v) || v < 1) return FVH_ERR_INVALID_ARGUMENT;
-    n[k] = (int32_t)v;
-    lo[k] = 0;
-    hi[k] = 1;
-    if (as_number(fvh::lua::lookup(mesh, "xmin" + idx), &v)) lo[k] = v;
-    if (as_number(fvh::lua::lookup(mesh, "xmax" + idx), &v)) hi[k] = v;
-  }
-  return fvh_host_mesh_box(dim, n, lo, hi, 0.0, 0, out);
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!in || !out) return FVH_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    const Value mesh = at(in, "hydro.mesh");
+    if (mesh.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
+    const Value type = fvh::lua::lookup(mesh, "type");
+    if (type.kind != Value::STRING || type.s != "box") return FVH_ERR_UNSUPPORTED;
+    const Value dims = fvh::lua::lookup(mesh, "dimensions");
+    if (dims.kind != Value::TABLE) return FVH_ERR_INVALID_ARGUMENT;
+    const int dim = (int)dims.t->array.size();
+    if (dim != 2 && dim != 3) return FVH_ERR_INVALID_ARGUMENT;
+    int32_t n[3];
+    double lo[3], hi[3];
+    for (int k = 0; k < dim; ++k) {
+      double v;
+      const std::string idx = "[" + std::to_string(k + 1) + "]";
+      // a whole number of cells that int32 holds (NaN and fractions refused)
+      if (!as_number(dims.t->array[k], &v) || !(v >= 1 && v <= 2147483647.0) ||
+          v != std::floor(v))
+        return FVH_ERR_INVALID_ARGUMENT;
+      n[k] = (int32_t)v;
+      lo[k] = 0;
+      hi[k] = 1;
+      if (as_number(fvh::lua::lookup(mesh, "xmin" + idx), &v)) lo[k] = v;
+      if (as_number(fvh::lua::lookup(mesh, "xmax" + idx), &v)) hi[k] = v;
+    }
+    return fvh_host_mesh_box(dim, n, lo, hi, 0.0, 0, out);
+  });
 }
 
 fvh_status fvh_input_initial_state(const fvh_input *in, const fvh_host_mesh *m,
                                    const fvh_params *p, double t, double *host_planes) {
-  if (!in || !m || !p || !host_planes || p->dim != m->dim) return FVH_ERR_INVALID_ARGUMENT;
-  const Value ics = at(in, "hydro.ics");
-  if (ics.kind != Value::FUNCTION) return FVH_ERR_INVALID_ARGUMENT;
-  const int D = m->dim, nc = m->nc;
-  std::vector<double> d(nc), v((size_t)D * nc), pr(nc);
-  fvh::lua::State &st = const_cast<fvh_input *>(in)->state;
-  try {
-    std::vector<Value> args(D + 1);
-    for (int c = 0; c < nc; ++c) {
-      for (int k = 0; k < D; ++k) args[k] = Value::number(m->cc[k][c]);
-      args[D] = Value::number(t);
-      const std::vector<Value> r = st.call(ics, args);
-      // initial_conditions (tasks.h:46-68): density, velocity, pressure
-      if (r.size() < 3 || r[0].kind != Value::NUMBER || r[1].kind != Value::TABLE ||
-          r[2].kind != Value::NUMBER)
-        return FVH_ERR_INVALID_ARGUMENT;
-      d[c] = r[0].n;
-      pr[c] = r[2].n;
-      for (int k = 0; k < D; ++k) {
-        const Value vk = r[1].t->get(Value::number(k + 1));
-        v[(size_t)k * nc + c] = vk.kind == Value::NUMBER ? vk.n : 0.0;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!in || !m || !p || !host_planes || p->dim != m->dim) return FVH_ERR_INVALID_ARGUMENT;
+    const Value ics = at(in, "hydro.ics");
+    if (ics.kind != Value::FUNCTION) return FVH_ERR_INVALID_ARGUMENT;
+    const int D = m->dim, nc = m->nc;
+    std::vector<double> d(nc), v((size_t)D * nc), pr(nc);
+    fvh::lua::State &st = const_cast<fvh_input *>(in)->state;
+    try {
+      std::vector<Value> args(D + 1);
+      for (int c = 0; c < nc; ++c) {
+        for (int k = 0; k < D; ++k) args[k] = Value::number(m->cc[k][c]);
+        args[D] = Value::number(t);
+        const std::vector<Value> r = st.call(ics, args);
+        // initial_conditions (tasks.h:46-68): density, velocity, pressure
+        if (r.size() < 3 || r[0].kind != Value::NUMBER || r[1].kind != Value::TABLE ||
+            r[2].kind != Value::NUMBER)
+          return FVH_ERR_INVALID_ARGUMENT;
+        d[c] = r[0].n;
+        pr[c] = r[2].n;
+        // positive, finite density and pressure (the reference asserts both,
+        // euler_eqns.h:342-343) and finite velocity
+        if (!(d[c] > 0) || !(pr[c] > 0) || !std::isfinite(d[c]) || !std::isfinite(pr[c]))
+          return FVH_ERR_INVALID_ARGUMENT;
+        for (int k = 0; k < D; ++k) {
+          const Value vk = r[1].t->get(Value::number(k + 1));
+          v[(size_t)k * nc + c] = vk.kind == Value::NUMBER ? vk.n : 0.0;
+          if (!std::isfinite(v[(size_t)k * nc + c])) return FVH_ERR_INVALID_ARGUMENT;
+        }
       }
+    } catch (const std::bad_alloc &) {
+      throw;  // FVH_ERR_OUT_OF_MEMORY
+    } catch (const std::exception &) {
+      return FVH_ERR_INVALID_ARGUMENT;
     }
-  } catch (const std::exception &) {
-    return FVH_ERR_INVALID_ARGUMENT;
-  }
-  return fvh_host_state_from_dvp(D, nc, p->gamma, p->cv, d.data(), v.data(), pr.data(),
-                                 host_planes);
+    return fvh_host_state_from_dvp(D, nc, p->gamma, p->cv, d.data(), v.data(), pr.data(),
+                                   host_planes);
+  });
 }
 
 }  // extern "C"

@@ -465,13 +465,13 @@ fvh_status fvh_host_mesh_box(int32_t dim, const int32_t *n, const double *lo,
                              const double *hi, double jitter, uint64_t seed,
                              fvh_host_mesh **out) {
   return fvh::no_throw([&]() -> fvh_status {
-    if (!out || !n || !lo || !hi || (dim != 2 && dim != 3) || jitter < 0 ||
-        jitter >= 0.5)
+    if (!out || !n || !lo || !hi || (dim != 2 && dim != 3) || !(jitter >= 0 && jitter < 0.5))
       return FVH_ERR_INVALID_ARGUMENT;
     int64_t nvx[3] = {1, 1, 1}, ncx[3] = {1, 1, 1};
     double h[3] = {0, 0, 0};
     for (int d = 0; d < dim; ++d) {
-      if (n[d] <= 0 || !(hi[d] > lo[d])) return FVH_ERR_INVALID_ARGUMENT;
+      if (n[d] <= 0 || !(hi[d] > lo[d]) || !std::isfinite(lo[d]) || !std::isfinite(hi[d]))
+        return FVH_ERR_INVALID_ARGUMENT;
       ncx[d] = n[d];
       nvx[d] = n[d] + 1;
       h[d] = (hi[d] - lo[d]) / n[d];

@@ -177,3 +177,29 @@ def test_hostile_inputs_are_refused_not_crashed():
         assert "stack overflow" in lines[name], (name, lines[name])
     for name in ("table_chain", "closure_chain", "many_locals"):
         assert lines[name] == "ok", (name, lines[name])
+
+
+def test_input_mesh_and_initial_state_values_are_checked():
+    """Box dimensions must be whole cell counts that int32 holds, extents
+    finite; the ics function must return positive, finite density and
+    pressure and finite velocity (the reference asserts rho > 0 and p > 0,
+    euler_eqns.h:342-343).  Each violation is an error status."""
+    base = "hydro = {{ mesh = {{ type = 'box', dimensions = {{{dims}}}, xmin = {{0, 0}}, " \
+           "xmax = {{{xmax}, 1}} }}, ics = function(x, y, t) return {ret} end }}"
+    good = dict(dims="4, 3", xmax="1", ret="1.0, {0.5, 0}, 2.0")
+    inp = H.Input(text=base.format(**good))
+    mesh = inp.mesh()
+    p, _, _ = inp.params(2)
+    s = inp.initial_state(mesh, p)
+    assert mesh.num_cells == 12 and np.all(s[0] == 1.0) and np.all(s[1] == 0.5)
+    for dims in ("4.5, 3", "0, 3", "-2, 3", "0/0, 3", "1e12, 3"):
+        with pytest.raises(H.FvhError):
+            H.Input(text=base.format(**dict(good, dims=dims))).mesh()
+    for xmax in ("1/0", "0/0", "-1"):
+        with pytest.raises(H.FvhError):
+            H.Input(text=base.format(**dict(good, xmax=xmax))).mesh()
+    for ret in ("0.0, {0, 0}, 1.0", "1.0, {0, 0}, -1.0", "0/0, {0, 0}, 1.0",
+                "1.0, {1/0, 0}, 1.0", "1.0, {0, 0}, 1/0"):
+        bad = H.Input(text=base.format(**dict(good, ret=ret)))
+        with pytest.raises(H.FvhError):
+            bad.initial_state(mesh, p)
