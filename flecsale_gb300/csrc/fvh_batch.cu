@@ -35,6 +35,14 @@ inline fvh_status from_cuda(cudaError_t e) {
   return FVH_ERR_CUDA;
 }
 
+// The launch shapes the batch kernels support: fvh_batch_set_shape accepts
+// only these, and a cached entry outside them (a damaged or hand-edited cache
+// file) is ignored rather than launched.
+bool batch_shape_ok(int block, int cells_per_thread, int schedule) {
+  return (block == 128 || block == 256) && cells_per_thread >= 1 && cells_per_thread <= 8 &&
+         (schedule == 0 || schedule == 1);
+}
+
 }  // namespace
 
 struct fvh_batch {
@@ -531,9 +539,7 @@ fvh_status fvh_batch_get_state(fvh_batch *b, int32_t k, double *host_planes, fvh
 
 fvh_status fvh_batch_set_shape(fvh_batch *b, int32_t block, int32_t cells_per_thread,
                                int32_t schedule) {
-  if (!b || (block != 128 && block != 256) || cells_per_thread < 1 || cells_per_thread > 8 ||
-      (schedule != 0 && schedule != 1))
-    return FVH_ERR_INVALID_ARGUMENT;
+  if (!b || !batch_shape_ok(block, cells_per_thread, schedule)) return FVH_ERR_INVALID_ARGUMENT;
   b->shape.block = block;
   b->shape.cells_per_thread = cells_per_thread;
   b->shape.schedule = schedule;
@@ -653,7 +659,8 @@ bool cache_lookup(const std::string &key, fvh::mixed::launch_shape *sh) {
   while (std::fgets(line, sizeof line, f)) {
     char k[512];
     int blk, cpt, sch;
-    if (std::sscanf(line, "%511s %d %d %d", k, &blk, &cpt, &sch) == 4 && key == k) {
+    if (std::sscanf(line, "%511s %d %d %d", k, &blk, &cpt, &sch) == 4 && key == k &&
+        batch_shape_ok(blk, cpt, sch)) {
       sh->block = blk;
       sh->cells_per_thread = cpt;
       sh->schedule = sch;
