@@ -146,3 +146,75 @@ def test_bench_conservation_totals(oracle_lib):
     assert st == 0
     assert abs(t1["mass"] - t0["mass"]) <= 1e-13 * t0["mass"]
     assert abs(t1["energy"] - t0["energy"]) <= 1e-13 * t0["energy"]
+
+
+def test_serving_loop_bookkeeping_with_a_fake_batch(monkeypatch):
+    """The continuous-batching loop on the host, with the device batch and
+    device meshes replaced by fakes that advance each problem's time: every
+    request finishes with its own state, running problems are carried into
+    each reassignment by the right keep index, and admissions wait for
+    capacity."""
+    DT = 0.01
+    assigns = []
+
+    class FakeDeviceMesh:
+        def __init__(self, mesh):
+            self.num_cells = mesh.num_cells
+
+    class FakeBatch:
+        def __init__(self, params, max_cells, max_faces, max_vertices, max_problems):
+            self.problems, self.meshes = [], []
+
+        def query(self, stream=None):
+            t = np.array([q["t"] for q in self.problems])
+            z = np.zeros(len(self.problems))
+            return t, z.astype(np.int32), (z - 1).astype(np.int64)
+
+        def get_state(self, k, stream=None):
+            return self.problems[k]["state"]
+
+        def set_state(self, k, planes, t, stream=None):
+            self.problems[k].update(t=t, state=planes)
+
+        def step(self, n, stream=None):
+            for q in self.problems:
+                q["t"] = min(q["t"] + n * DT, q["t_end"])
+                q["steps"] += n
+
+        def close(self):
+            pass
+
+    def fake_assign(batch, dmeshes, cfl, final_time, keep=None, stream=None):
+        new = []
+        for k, dm in enumerate(dmeshes):
+            if keep[k] >= 0:
+                carried = batch.problems[keep[k]]
+                assert carried["dm"] is dm  # the same request's problem is carried
+                new.append(carried)
+            else:
+                new.append({"t": None, "t_end": final_time[k], "dm": dm, "steps": 0})
+        assigns.append((len(dmeshes), sum(dm.num_cells for dm in dmeshes)))
+        batch.problems, batch.meshes = new, list(dmeshes)
+
+    monkeypatch.setattr(H, "Batch", FakeBatch)
+    monkeypatch.setattr(H, "DeviceMesh", FakeDeviceMesh)
+    monkeypatch.setattr(H, "batch_assign_device", fake_assign)
+    reqs = [serve.Request(k, 0.002 * k, side, "sod", t_end)
+            for k, (side, t_end) in enumerate([(12, 0.05), (10, 0.2), (14, 0.1), (8, 0.05),
+                                               (12, 0.3), (9, 0.08)])]
+    p = serve.server_params()
+    srv = serve.Server(p, max_cells=300, max_faces=10**6, max_vertices=10**6, max_problems=3,
+                       steps_per_launch=2, build_threads=2)
+    try:
+        out = srv.run(reqs, time_limit=60.0)
+    finally:
+        srv.close()
+    assert out["requests_done"] == len(reqs) and out["failed"] == 0
+    assert out["reassignments"] == len(assigns) >= 3
+    assert all(n <= 3 and cells <= 300 for n, cells in assigns)  # within every capacity
+    for r in out["done"]:
+        assert abs(r.t_final - r.t_end) <= 1e-12 * r.t_end  # ran to its own end time
+        assert r.result is r.state0                       # and returned its own state
+        assert r.admitted >= 0 and r.finished >= r.admitted
+    # 6 requests, 832 cells in all, through a 300-cell batch: some had to wait for a slot
+    assert any(r.admitted > min(q.finished for q in reqs) for r in reqs)
