@@ -705,7 +705,8 @@ class Input:
         else:
             code = lib().fvh_input_load_string(text.encode(), err, 512, C.byref(self._h))
         if code != 0:
-            raise FvhError(code, err.value.decode() or "fvh_input_load")
+            # the message may quote bytes of the file that are not UTF-8
+            raise FvhError(code, err.value.decode(errors="replace") or "fvh_input_load")
 
     def number(self, path: str) -> float:
         v = C.c_double()
@@ -715,7 +716,7 @@ class Input:
     def string(self, path: str) -> str:
         buf = C.create_string_buffer(4096)
         check(lib().fvh_input_string(self._h, path.encode(), buf, 4096), path)
-        return buf.value.decode()
+        return buf.value.decode(errors="replace")
 
     def params(self, dim: int, **kw) -> tuple:
         """(Params, max_steps, output_freq): reference defaults for dim, then the file."""

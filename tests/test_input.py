@@ -203,3 +203,17 @@ def test_input_mesh_and_initial_state_values_are_checked():
         bad = H.Input(text=base.format(**dict(good, ret=ret)))
         with pytest.raises(H.FvhError):
             bad.initial_state(mesh, p)
+
+
+def test_mutated_input_files_are_loaded_or_refused():
+    """Random byte mutations of the shipped input files either load or are
+    refused with an error status, never crash (in a child process); an error
+    message quoting a byte that is not UTF-8 still reaches Python as FvhError."""
+    with pytest.raises(H.FvhError):
+        H.Input(text="x = \x80\nhydro = {}")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([os.sys.executable, os.path.join(root, "tests", "_lua_fuzz.py"), "5", "1500"],
+                       capture_output=True, text=True, timeout=600, cwd=root,
+                       env=dict(os.environ, PYTHONPATH=root))
+    assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
+    assert "refused" in r.stdout
