@@ -119,21 +119,41 @@ fvh_status fvh_input_string(const fvh_input *in, const char *path, char *buf, si
 
 fvh_status fvh_input_params(const fvh_input *in, fvh_params *p, int64_t *max_steps,
                             int64_t *output_freq) {
-  if (!in || !p) return FVH_ERR_INVALID_ARGUMENT;
-  double v;
-  if (as_number(at(in, "hydro.CFL"), &v)) p->cfl = v;
-  if (as_number(at(in, "hydro.final_time"), &v)) p->final_time = v;
-  if (max_steps && as_number(at(in, "hydro.max_steps"), &v)) *max_steps = (int64_t)v;
-  if (output_freq && as_number(at(in, "hydro.output_freq"), &v)) *output_freq = (int64_t)v;
-  const Value eos = at(in, "hydro.eos");
-  if (eos.kind == Value::TABLE) {
-    const Value type = fvh::lua::lookup(eos, "type");
-    if (type.kind != Value::STRING || type.s != "ideal_gas")
-      return FVH_ERR_UNSUPPORTED;  // inputs.h:129-131 "Unknown eos type"
-    if (as_number(fvh::lua::lookup(eos, "gas_constant"), &v)) p->gamma = v;
-    if (as_number(fvh::lua::lookup(eos, "specific_heat"), &v)) p->cv = v;
-  }
-  return FVH_OK;
+  return fvh::no_throw([&]() -> fvh_status {
+    if (!in || !p) return FVH_ERR_INVALID_ARGUMENT;
+    // values are checked before they are stored: counts are whole and
+    // non-negative (they convert to int64 exactly), CFL and the EOS constants
+    // positive and finite (gamma > 1), the final time not NaN
+    double v;
+    auto count = [&](const char *key, int64_t *out) -> bool {
+      if (!out || !as_number(at(in, key), &v)) return true;
+      if (!(v >= 0 && v <= 9.0e18) || v != std::floor(v)) return false;
+      *out = (int64_t)v;
+      return true;
+    };
+    fvh_params q = *p;
+    if (as_number(at(in, "hydro.CFL"), &v)) q.cfl = v;
+    if (as_number(at(in, "hydro.final_time"), &v)) q.final_time = v;
+    const Value eos = at(in, "hydro.eos");
+    if (eos.kind == Value::TABLE) {
+      const Value type = fvh::lua::lookup(eos, "type");
+      if (type.kind != Value::STRING || type.s != "ideal_gas")
+        return FVH_ERR_UNSUPPORTED;  // inputs.h:129-131 "Unknown eos type"
+      if (as_number(fvh::lua::lookup(eos, "gas_constant"), &v)) q.gamma = v;
+      if (as_number(fvh::lua::lookup(eos, "specific_heat"), &v)) q.cv = v;
+    }
+    if (!(q.cfl > 0) || !std::isfinite(q.cfl) || std::isnan(q.final_time) || !(q.gamma > 1) ||
+        !std::isfinite(q.gamma) || !(q.cv > 0) || !std::isfinite(q.cv))
+      return FVH_ERR_INVALID_ARGUMENT;
+    int64_t ms = max_steps ? *max_steps : 0, of = output_freq ? *output_freq : 0;
+    if (!count("hydro.max_steps", max_steps ? &ms : nullptr) ||
+        !count("hydro.output_freq", output_freq ? &of : nullptr))
+      return FVH_ERR_INVALID_ARGUMENT;
+    *p = q;
+    if (max_steps) *max_steps = ms;
+    if (output_freq) *output_freq = of;
+    return FVH_OK;
+  });
 }
 
 fvh_status fvh_input_mesh(const fvh_input *in, fvh_host_mesh **out) {

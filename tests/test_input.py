@@ -217,3 +217,24 @@ def test_mutated_input_files_are_loaded_or_refused():
                        env=dict(os.environ, PYTHONPATH=root))
     assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
     assert "refused" in r.stdout
+
+
+def test_input_parameter_values_are_checked():
+    """Out-of-range values in the hydro table are refused (and p is left as
+    it was); numeric strings such as output_freq = "1e6" still read."""
+    ok = H.Input(text="hydro = { CFL = 0.3, final_time = 0.1, max_steps = 7, output_freq = '1e6',"
+                      " eos = { type = 'ideal_gas', gas_constant = 1.6, specific_heat = 2 } }")
+    p, ms, of = ok.params(2)
+    assert (p.cfl, p.final_time, p.gamma, p.cv, ms, of) == (0.3, 0.1, 1.6, 2.0, 7, 1000000)
+    bad = ["CFL = -1", "CFL = 0/0", "CFL = 1/0", "final_time = 0/0", "max_steps = -1",
+           "max_steps = 1.5", "max_steps = 0/0", "max_steps = 1e300", "output_freq = -3",
+           "eos = { type = 'ideal_gas', gas_constant = 1 }",
+           "eos = { type = 'ideal_gas', specific_heat = 0 }"]
+    for entry in bad:
+        inp = H.Input(text=f"hydro = {{ {entry} }}")
+        with pytest.raises(H.FvhError) as e:
+            inp.params(2)
+        assert e.value.code == H.ERR_INVALID_ARGUMENT, entry
+    with pytest.raises(H.FvhError) as e:
+        H.Input(text="hydro = { eos = { type = 'stiffened_gas' } }").params(2)
+    assert e.value.code == H.ERR_UNSUPPORTED
