@@ -10,9 +10,13 @@ Barth-Jespersen vertex limiter; HLLC fluxes; transmissive boundaries (with the
 reference's reflecting walls the receding SW quadrant empties the corner and
 the state goes negative within ~10-80 steps); CFL 0.4.  Synthetic data.
 
-The headline value is the mixed-precision form (FP32 reconstruction + flux,
-FP64 state/update/dt); the plain FP64 path is reported beside it with the
-relative L1 density/energy error of mixed vs FP64 after the same steps.
+The headline value is the plain FP64 path, whose arithmetic is bitwise the
+reference's (the same precision as the reference CPU solver it is compared
+with).  Beside it: the mixed-precision form (FP32 reconstruction + flux, FP64
+state/update/dt) with its L1/Linf density and energy errors against FP64 after
+the same steps; the 512-problem batch; the served request stream (60 s of
+Poisson arrivals); the 192^3 3D shock box in both forms; and the CPU baseline.
+Every form is also timed end to end through the C ABI from host memory.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -45,15 +49,29 @@ WORKLOAD = ("2D four-quadrant Riemann problem, 1024x1024 quads on [0,1]^2 jitter
             "HLLC, transmissive boundaries, CFL 0.4, one step = dt + predictor + corrector")
 
 
+# the workload's solver settings (the oracle takes the same keywords)
+ORACLE_KW = dict(flux="hllc", limiter="barth_jespersen", order=2, swap=True, cfl=0.4,
+                 final_time=1.0e9, boundary="outflow")
+
+
 def build_problem(n_side: int = N_SIDE):
     import flecsale_gb300.hydro as H
     mesh = H.HostMesh.box(2, (n_side, n_side), [0, 0], [1, 1], JITTER, SEED)
-    kw = dict(flux="hllc", limiter="barth_jespersen", order=2, swap=True, cfl=0.4,
-              final_time=1.0e9, boundary="outflow")
-    p64 = H.make_params(2, precision="fp64", **kw)
-    p32 = H.make_params(2, precision="mixed", **kw)
+    p64 = H.make_params(2, precision="fp64", **ORACLE_KW)
+    p32 = H.make_params(2, precision="mixed", **ORACLE_KW)
     state0 = H.initial_state("four_quadrant", mesh, p64)
     return H, mesh, p64, p32, state0
+
+
+def workload_config(mesh) -> dict:
+    """The bench line's config: the same dict for this repository's arm and
+    the reference arm (the per-step working set, FP64 state + gradients +
+    fluxes + mesh, is far above the 129 MB L2, so no flush is needed)."""
+    ws_mb = 1572 * mesh.num_cells / 2 / 1e6
+    return {"workload": WORKLOAD, "cells": mesh.num_cells, "faces": mesh.num_faces,
+            "form": "plain FP64",
+            "l2": (f"no flush: per-stage working set ~{ws_mb:.0f} MB > 129 MB L2" if ws_mb > 129
+                   else f"small test size: per-stage working set ~{ws_mb:.0f} MB fits in L2")}
 
 
 def conservation_totals(mesh, state) -> dict:
@@ -151,13 +169,15 @@ def peaks():
 
 
 def ncu_traffic() -> dict:
-    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary: {form:kernel: {"bytes", "commit", ...}}."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(path) as fh:
-            return json.load(fh)
+            d = json.load(fh)
     except Exception:
         return {}
+    return {k: (v if isinstance(v, dict) else {"bytes": v}) for k, v in d.items()}
 
 
 def ncu_pipes() -> dict:
@@ -226,19 +246,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (C++ restatement of the reference, OpenMP)
 # ---------------------------------------------------------------------------
-def cpu_baseline(mesh, params, state0, budget_s: float = 12.0, max_steps: int = 400) -> dict:
+def cpu_baseline(n_side: int, budget_s: float = 12.0, max_steps: int = 400) -> dict:
     """The oracle (the reference's tasks restated in C++/OpenMP) on the host
-    cores: all threads (the reported value) and one thread."""
+    cores, on the same workload built by the oracle's own mesh builder: all
+    threads (the reported value) and one thread."""
     import oracle
-    from tests import _util as U
     O = oracle.load()
+    mesh = oracle.BoxMesh2D(n_side, n_side, (0.0, 0.0), (1.0, 1.0), JITTER, SEED)
+    p64 = oracle.params(2, **ORACLE_KW)
+    state0 = oracle.four_quadrant_state(mesh)
 
     def sample(budget):
         s = state0.copy()
-        U.oracle_run(O, mesh, s, params, 1)  # warm-up step
+        oracle.run(mesh, s, p64, 1)  # warm-up step
         n, t0 = 0, time.perf_counter()
         while n < max_steps and (time.perf_counter() - t0) < budget:
-            U.oracle_run(O, mesh, s, params, 1)
+            oracle.run(mesh, s, p64, 1)
             n += 1
         return n, time.perf_counter() - t0
 
@@ -249,7 +272,7 @@ def cpu_baseline(mesh, params, state0, budget_s: float = 12.0, max_steps: int = 
     n1, dt1 = sample(budget_s / 3)
     O.oracle_set_threads(0)
     return {"value": mesh.num_cells * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} full time steps of the {N_SIDE}x{N_SIDE} workload in {dt:.1f} s "
+            "sample": f"{n} full time steps of the {n_side}x{n_side} workload in {dt:.1f} s "
                       f"(FP64, HLLC; oracle/hydro_oracle.cpp, -O2, OpenMP)",
             "one_thread": {"value": mesh.num_cells * n1 / dt1, "cores": 1,
                            "sample": f"{n1} steps in {dt1:.1f} s"}}
@@ -280,19 +303,26 @@ def max_over_ranks(dist, value: float, device: str = "cuda") -> float:
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference solver (the
+    reference itself cannot be built) on the same workload, all host threads,
+    rank 0 only.  Mesh, initial state and parameters come from the oracle's own
+    builders, so this process never loads the product library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    H, mesh, p64, _, state0 = build_problem(args.n)
     import oracle
-    from tests import _util as U
+    mesh = oracle.BoxMesh2D(args.n, args.n, (0.0, 0.0), (1.0, 1.0), JITTER, SEED)
+    p64 = oracle.params(2, **ORACLE_KW)
+    s = oracle.four_quadrant_state(mesh)
     O = oracle.load()
-    s = state0.copy()
+    O.oracle_set_threads(0)
     for _ in range(args.warmup):
-        U.oracle_run(O, mesh, s, p64, 1)
+        oracle.run(mesh, s, p64, 1)
     t0 = time.perf_counter()
-    U.oracle_run(O, mesh, s, p64, args.steps)
+    st, _, _ = oracle.run(mesh, s, p64, args.steps)
     dt = time.perf_counter() - t0
+    if st != 0:
+        raise RuntimeError(f"reference arm: oracle status {st}")
     cores = int(O.oracle_max_threads())
     value = mesh.num_cells * args.steps / dt
     line = {
@@ -300,10 +330,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": mesh.num_cells, "faces": mesh.num_faces,
-                   "form": "reference CPU solver restated (oracle), FP64"},
+        "config": workload_config(mesh),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full time steps of the workload, all host threads"},
+                         "sample": f"{args.steps} full time steps of the workload after "
+                                   f"{args.warmup} warm-up steps, all host threads "
+                                   "(oracle/hydro_oracle.cpp, -O2, OpenMP; mesh from "
+                                   "oracle/box_mesh.cpp)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -475,6 +507,20 @@ def timed_steps(torch, solver, dstate, stream, K, dist):
     return ms
 
 
+def e2e_steps(solver, dstate, host, steps, warmup, stream, dist) -> float:
+    """Seconds for `steps` calls of fvh_solver_advance_host, one step each,
+    pinned host state in and out (max over ranks)."""
+    t_sim = 0.0
+    for _ in range(warmup):
+        t_sim = solver.advance_host(dstate, host, 1, t_sim, stream)
+    if dist:
+        dist.barrier()
+    w0 = time.perf_counter()
+    for _ in range(steps):
+        t_sim = solver.advance_host(dstate, host, 1, t_sim, stream)
+    return max_over_ranks(dist, time.perf_counter() - w0)
+
+
 def run_ours(args):
     import torch
     dist, ws, rank, local = dist_setup("nccl")
@@ -483,11 +529,10 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     dmesh = H.DeviceMesh(mesh)
     nc = mesh.num_cells
-    results = {}
-    finals = {}
-    shape = None
+    results, finals, shape = {}, {}, None
+    host = torch.empty((7, nc), dtype=torch.float64, pin_memory=True).numpy()
     with ClockSampler(local) as clk:
-        for form, params in (("mixed", p32), ("fp64", p64)):
+        for form, params in (("fp64", p64), ("mixed", p32)):
             dstate = H.DeviceState(2, nc)
             solver = H.Solver(dmesh, params)
             dstate.upload(state0, stream)
@@ -505,24 +550,12 @@ def run_ours(args):
             if code != 0:
                 raise RuntimeError(f"{form}: device status {code} at cell {cell}")
             finals[form] = dstate.download(stream)
+            # end to end through the C ABI from pinned host memory, same workload
+            host[:] = state0[:7]
+            e2e_s = e2e_steps(solver, dstate, host, args.steps, args.warmup, stream, dist)
             results[form] = {"ms": ms, "launches": solver.launches_per_run(args.steps), "t": t,
-                             "solver": solver, "state": dstate}
+                             "solver": solver, "state": dstate, "e2e_s": e2e_s}
     clocks = clk.summary()
-
-    # end to end through the C ABI with host buffers (mixed form)
-    r = results["mixed"]
-    host = torch.empty((7, nc), dtype=torch.float64, pin_memory=True).numpy()
-    host[:] = state0[:7]
-    t_sim = 0.0
-    for _ in range(args.warmup):
-        t_sim = r["solver"].advance_host(r["state"], host, 1, t_sim, stream)
-    if dist:
-        dist.barrier()
-    w0 = time.perf_counter()
-    for _ in range(args.steps):
-        t_sim = r["solver"].advance_host(r["state"], host, 1, t_sim, stream)
-    e2e_s = time.perf_counter() - w0
-    e2e_s = max_over_ranks(dist, e2e_s)
 
     # per-kernel timings (CUDA events between launches on the stream)
     prof = {f: results[f]["solver"].profile(results[f]["state"], 10, stream) for f in results}
@@ -533,69 +566,92 @@ def run_ours(args):
         return 0
 
     hbm, peak_kind = peaks()
-    traffic = ncu_traffic()
+    traffic, pipes = ncu_traffic(), ncu_pipes()
 
     def roofline(form):
+        """Dominant kernel of the form: algorithmic bytes per launch over its
+        duration.  The per-kernel event times of fvh_solver_profile are taken
+        with an event between every two launches, which serialises the step
+        a little; each kernel's duration here is its profiled share of the
+        in-run step time (ms_per_step of the timed run)."""
         ab = algorithmic_bytes(mesh, form)
         p = prof[form]
         if "face_colour" in p:  # one launch per colour: the stage's bytes over its launches
             ab["face_colour"] = ab["face_colour_stage"] / (p["face_colour"][1] / 2)
+        profiled_step = sum(v[0] * v[1] for v in p.values())
+        in_run_step = results[form]["ms"] / args.steps
+        scale = in_run_step / profiled_step
         dom = max(p, key=lambda k: p[k][0] * p[k][1])
-        achieved = ab[dom] / (p[dom][0] * 1e-3) / 1e9
-        step_ms = sum(v[0] * v[1] for v in p.values())
-        return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
-                "traffic": traffic.get(f"{form}:{dom}"),
-                "algorithmic_bytes_per_launch": ab[dom],
-                "kernels": {k: {"mean_ms": v[0], "launches_per_step": v[1],
-                                "share": v[0] * v[1] / step_ms,
-                                "achieved_gbs": ab[k] / (v[0] * 1e-3) / 1e9}
-                            for k, v in p.items()}}
+        dur = p[dom][0] * scale
+        achieved = ab[dom] / (dur * 1e-3) / 1e9
+        tr = traffic.get(f"{form}:{dom}", {})
+        out = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+               "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
+               "traffic": tr.get("bytes"), "traffic_commit": tr.get("commit"),
+               "algorithmic_bytes_per_launch": ab[dom],
+               "duration_ms": dur,
+               "duration_note": "profiled per-kernel event time x (in-run ms_per_step / "
+                                f"profiled step {profiled_step:.4f} ms = {scale:.3f})",
+               "kernels": {k: {"duration_ms": v[0] * scale, "launches_per_step": v[1],
+                               "share": v[0] * v[1] / profiled_step,
+                               "achieved_gbs": ab[k] / (v[0] * scale * 1e-3) / 1e9,
+                               "frac": ab[k] / (v[0] * scale * 1e-3) / 1e9 / hbm,
+                               "fp64_pipe_active": pipes.get(f"{form}:{k}", {}).get("fp64")}
+                           for k, v in p.items()}}
+        return out
 
     zu = lambda ms: ws * nc * args.steps / (ms * 1e-3)
     m, f = finals["mixed"], finals["fp64"]
     l1 = lambda a, b: float(np.abs(a - b).sum() / np.abs(b).sum())
     E = lambda s: s[0] * (s[3] + 0.5 * (s[1] ** 2 + s[2] ** 2))
-    # the step reads d, v, e, p, a from the host planes (T is not an input) and
-    # writes all seven planes back
-    in_bytes, out_bytes = 6 * 8 * nc, 7 * 8 * nc
+
+    def e2e(form):
+        if form == "fp64":  # upload of the 7 planes, steps, download of the 7 planes
+            bi, bo = 7 * 8 * nc, 7 * 8 * nc
+            call = ("fvh_solver_advance_host (pinned host state: 7 planes copied in, 1 step, "
+                    "7 planes copied out)")
+        else:  # the step reads d, v, e, p, a from the host planes and writes all 7
+            bi, bo = 6 * 8 * nc, 7 * 8 * nc
+            call = ("fvh_solver_advance_host (pinned host state in, 1 step, host state out; the "
+                    "first and last kernels access the host planes directly)")
+        return {"value": ws * nc * args.steps / results[form]["e2e_s"], "unit": UNIT,
+                "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "call": call}
+
+    fp64_roof = roofline("fp64")
+    fp64_roof["pipe_bound"] = "fp64"
+    fp64_roof["note"] = ("the FP64 kernels are bound by GB300's FP64 pipe (2 FP64 operations "
+                         "per clock per SM); fp64_pipe_active per kernel is the ncu figure "
+                         "(profiles/pipe_utilization.json)")
     line = {
         "metric": METRIC,
-        "value": zu(results["mixed"]["ms"]),
+        "value": zu(results["fp64"]["ms"]),
         "unit": UNIT,
         "n_gpus": ws,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": results["mixed"]["ms"] / args.steps,
+        "ms_per_step": results["fp64"]["ms"] / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32+f64",
+        "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": nc, "faces": mesh.num_faces,
-                   "form": "mixed: FP32 reconstruction + Riemann flux, compensated FP32 face "
-                           "sums, double-float increments onto the FP64 state, FP64 dt",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
-                   "l2": "no flush: per-step working set (state, FP32 pack/gradients, mesh) "
-                         f"~{per_zone_update_bytes(mesh, 'mixed') * nc / 2 / 1e6:.0f} MB per stage > 129 MB L2",
-                   "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "mixed"),
-                   "launch_shape": shape},
+        "config": workload_config(mesh),
+        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+        "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "fp64"),
         "clocks": clocks,
-        "e2e": {"value": ws * nc * args.steps / e2e_s, "unit": UNIT,
-                "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes,
-                "call": "fvh_solver_advance_host (pinned host state in, 1 step, host state out; the "
-                        "first and last kernels access the host planes directly)"},
-        "gpu_launches": results["mixed"]["launches"],
-        "roofline": roofline("mixed"),
-        "plain_fp64": {"value": zu(results["fp64"]["ms"]),
-                       "ms_per_step": results["fp64"]["ms"] / args.steps,
-                       "gpu_launches": results["fp64"]["launches"],
-                       "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "fp64"),
-                       "roofline": dict(roofline("fp64"), fp64_pipe_active=ncu_pipes().get(
-                           "fp64:gradients", {}).get("fp64"),
-                           note="FP64-pipe bound: GB300 issues 2 FP64 operations per clock "
-                                "per SM; fp64_pipe_active is the ncu figure of the dominant "
-                                "kernel (profiles/fp64_gradients_1024sq_four_quadrant.md)")},
+        "e2e": e2e("fp64"),
+        "gpu_launches": results["fp64"]["launches"],
+        "roofline": fp64_roof,
+        "mixed": {"value": zu(results["mixed"]["ms"]),
+                  "ms_per_step": results["mixed"]["ms"] / args.steps,
+                  "dtype": "f32+f64",
+                  "form": "FP32 reconstruction + Riemann flux, compensated FP32 face sums, "
+                          "double-float increments onto the FP64 state, FP64 dt",
+                  "gpu_launches": results["mixed"]["launches"],
+                  "launch_shape": shape,
+                  "algorithmic_bytes_per_zone_update": per_zone_update_bytes(mesh, "mixed"),
+                  "e2e": e2e("mixed"),
+                  "roofline": roofline("mixed")},
         "mixed_over_fp64": results["fp64"]["ms"] / results["mixed"]["ms"],
         "accuracy": {"steps": args.warmup + args.steps,
                      "l1_density_mixed_vs_fp64": l1(m[0], f[0]),
@@ -608,19 +664,48 @@ def run_ours(args):
                          "fp64": conservation_totals(mesh, f),
                          "mixed": conservation_totals(mesh, m)},
     }
+    for form in ("fp64", "mixed"):
+        results[form]["solver"].close()
+        del results[form]["state"]
     if not args.no_batch:
         line["batched"] = run_batched(torch, stream, min(args.steps, 50), args.warmup)
-        line["batched_over_fp64"] = line["batched"]["value"] / line["plain_fp64"]["value"]
+        line["batched_over_fp64"] = line["batched"]["value"] / line["value"]
         if args.serve_seconds > 0:
             line["serving"] = run_serving(torch, stream, line["batched"]["value"],
                                           args.serve_seconds)
-    if args.with_3d:
-        line["shock_box_3d"] = run_3d(torch, stream)
+    if not args.no_3d:
+        line["shock_box_3d"] = run_3d(torch, stream, args.n3d, args.steps3d)
     if ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mesh, p64, state0)
+        line["cpu_baseline"] = cpu_baseline(args.n)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+    return 0
+
+
+def run_only_2d(args):
+    """One form of the 2D workload alone: warm-up steps, then the timed steps
+    in one fvh_solver_run (fixed launch shape for the mixed form if --shape)."""
+    import torch
+    torch.cuda.set_device(0)
+    H, mesh, p64, p32, state0 = build_problem(args.n)
+    stream = torch.cuda.Stream()
+    params = p64 if args.only_2d == "fp64" else p32
+    dmesh, dstate = H.DeviceMesh(mesh), H.DeviceState(2, mesh.num_cells)
+    solver = H.Solver(dmesh, params)
+    dstate.upload(state0, stream)
+    solver.reset(0.0, stream)
+    if args.only_2d == "mixed" and args.shape:
+        solver.set_shape(*(int(v) for v in args.shape.split(",")))
+    for _ in range(args.warmup):
+        solver.step(dstate, stream)
+    ms = timed_steps(torch, solver, dstate, stream, args.steps, None)
+    code, t, cell = solver.status(stream)
+    if code != 0:
+        raise RuntimeError(f"{args.only_2d}: device status {code} at cell {cell}")
+    print(json.dumps({"form": args.only_2d, "cells": mesh.num_cells, "steps": args.steps,
+                      "ms_per_step": ms / args.steps,
+                      "value": mesh.num_cells * args.steps / (ms * 1e-3)}), flush=True)
     return 0
 
 
@@ -635,11 +720,16 @@ def main():
     ap.add_argument("--shape", default="",
                     help="fixed mixed launch shape 'block,cells_per_thread,schedule' "
                          "instead of autotuning (profiling runs)")
-    ap.add_argument("--with-3d", action="store_true",
-                    help="also run the 192^3 3D shock box, FP64 vs mixed (100 steps)")
-    ap.add_argument("--serve-seconds", type=float, default=12.0,
+    ap.add_argument("--no-3d", action="store_true",
+                    help="skip the 3D shock box (192^3, FP64 vs mixed, 100 steps)")
+    ap.add_argument("--n3d", type=int, default=192, help="3D shock box side (default 192)")
+    ap.add_argument("--steps3d", type=int, default=100, help="3D shock box steps (default 100)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the serving run (0 skips it)")
     ap.add_argument("--n", type=int, default=N_SIDE, help="mesh side (default 1024)")
+    ap.add_argument("--only-2d", choices=["fp64", "mixed"], default="",
+                    help="run only one form of the 2D workload (warm-up + steps) and print its "
+                         "time (profiling of that form's kernels)")
     ap.add_argument("--only-3d", type=int, default=0, metavar="N",
                     help="run only the 3D shock box on an N^3 mesh for --steps steps and print "
                          "its record (profiling of the 3D kernels)")
@@ -653,6 +743,8 @@ def main():
         torch.cuda.set_device(0)
         print(json.dumps(run_3d(torch, torch.cuda.Stream(), args.only_3d, args.steps)), flush=True)
         return 0
+    if args.only_2d:
+        return run_only_2d(args)
     return run_ours(args)
 
 

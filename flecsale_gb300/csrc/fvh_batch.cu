@@ -114,6 +114,19 @@ void set_state_view(fvh_batch *b) {
   s.sound_speed = base + stride * k++;
 }
 
+// A reassignment that failed after it began to overwrite the batch's device
+// arrays leaves no consistent problem set: the batch is emptied (no problems,
+// no graphs), so fvh_batch_step refuses to run until the next successful
+// assignment instead of stepping a mix of old and new meshes.
+fvh_status fail_assign(fvh_batch *b, cudaError_t e) {
+  drop_graphs(b);
+  b->nproblems = 0;
+  b->first_cell.assign(1, 0);
+  std::memset(&b->view, 0, sizeof(b->view));
+  b->view.dim = b->dim;
+  return from_cuda(e);
+}
+
 }  // namespace
 
 extern "C" {
@@ -199,9 +212,15 @@ fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const 
     if (n > b->max_problems) return FVH_ERR_CAPACITY;
     for (int k = 0; k < n; ++k)
       if (!meshes[k] || meshes[k]->dim != b->dim || !(cfl[k] > 0)) return FVH_ERR_INVALID_ARGUMENT;
+    // a carried problem must exist and keep its cell count; checked before any
+    // device memory is touched
     if (keep)
-      for (int k = 0; k < n; ++k)
+      for (int k = 0; k < n; ++k) {
         if (keep[k] >= b->nproblems) return FVH_ERR_INVALID_ARGUMENT;
+        if (keep[k] >= 0 &&
+            b->first_cell[keep[k] + 1] - b->first_cell[keep[k]] != meshes[k]->nc)
+          return FVH_ERR_INVALID_ARGUMENT;
+      }
     fvh_host_mesh *cat = nullptr;
     fvh_status r = fvh_host_mesh_concat(n, meshes, &cat);
     if (r != FVH_OK) return r;
@@ -228,11 +247,7 @@ fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const 
     for (int k = 0; k < n && e == cudaSuccess; ++k) {
       if (!keep || keep[k] < 0) continue;
       const int o = keep[k];
-      const int64_t ncells = old_first[o + 1] - old_first[o];
-      if (ncells != meshes[k]->nc) {
-        e = cudaErrorInvalidValue;
-        break;
-      }
+      const int64_t ncells = old_first[o + 1] - old_first[o];  // == meshes[k]->nc
       times[k] = b->h_t[o];
       for (int pl = 0; pl < 5 + D && e == cudaSuccess; ++pl)
         e = cudaMemcpyAsync(b->state_buf[nxt] + pl * stride + first[k],
@@ -250,7 +265,8 @@ fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const 
     up(b->nb, cat->nb.data(), sizeof(int32_t) * cat->nb.size());
     up(b->cv_off, cat->cv_off.data(), sizeof(int32_t) * cat->cv_off.size());
     up(b->cv, cat->cv.data(), sizeof(int32_t) * cat->cv.size());
-    fvh_mesh_view &v = b->view;
+    // the new view is committed to the batch only once everything succeeded
+    fvh_mesh_view v;
     std::memset(&v, 0, sizeof(v));
     v.dim = D;
     v.num_cells = cat->nc;
@@ -296,7 +312,8 @@ fvh_status fvh_batch_assign(fvh_batch *b, int32_t n, const fvh_host_mesh *const 
     if (e == cudaSuccess) e = cudaMemsetAsync(b->status, 0xff, sizeof(fvh_device_status) * n, st);
     if (e == cudaSuccess) e = fvh::mixed::setup_geometry(b->ws, v, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // before the host arrays are freed
-    if (e != cudaSuccess) return from_cuda(e);
+    if (e != cudaSuccess) return fail_assign(b, e);
+    b->view = v;
     b->cur = nxt;
     set_state_view(b);
     b->first_cell = std::move(first);
@@ -440,8 +457,8 @@ fvh_status fvh_batch_assign_device(fvh_batch *b, int32_t n,
       for (int k = 0; k < n; ++k)
         if (keep[k] >= 0) times[k] = b->h_t[keep[k]];
     }
-    // destination view
-    fvh_mesh_view &v = b->view;
+    // destination view, committed to the batch only once everything succeeded
+    fvh_mesh_view v;
     std::memset(&v, 0, sizeof(v));
     v.dim = D;
     v.num_cells = (int32_t)nc;
@@ -499,7 +516,8 @@ fvh_status fvh_batch_assign_device(fvh_batch *b, int32_t n,
     if (e == cudaSuccess) e = fvh::mixed::setup_geometry(b->ws, v, st);
     if (d_src) cudaFreeAsync(d_src, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return from_cuda(e);
+    if (e != cudaSuccess) return fail_assign(b, e);
+    b->view = v;
     b->cur = nxt;
     set_state_view(b);
     b->first_cell = std::move(first);

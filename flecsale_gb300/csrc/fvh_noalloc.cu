@@ -18,11 +18,19 @@
 // All calls share the one array.  Each call writes every partial it later reads
 // before reading it, so nothing has to be cleared between calls, but two calls
 // whose kernels overlap on the GPU (for example on two streams) race on it.
+//
+// The arguments are checked exactly as fvh_evaluate_time_step checks them, and
+// CUDA errors map to the same status codes.  The kernels are the same; only
+// the number of blocks differs above kDtMaxBlocks blocks (fvh_evaluate_time_step
+// then strides each block over more cells), and the largest of the per-block
+// maxima does not depend on how the cells were split, so both entry points
+// give the same dt for every state without a NaN.
 #include <cuda_runtime.h>
 
 #include <atomic>
 
 #include "flecsale_gb300.h"
+#include "fvh_checks.h"
 #include "fvh_kernels.h"
 
 namespace {
@@ -44,7 +52,8 @@ fvh_status partials_for_current_device(double **out) {
   double *p = g_partials_addr[dev].load(std::memory_order_acquire);
   if (!p) {
     const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_dt_partials);
-    if (e != cudaSuccess || !p) return FVH_ERR_CUDA;
+    if (e != cudaSuccess) return fvh::from_cuda(e);
+    if (!p) return FVH_ERR_CUDA;
     g_partials_addr[dev].store(p, std::memory_order_release);
   }
   *out = p;
@@ -63,14 +72,9 @@ fvh_status fvh_evaluate_time_step_noalloc(const fvh_mesh_view *mesh,
                                           const double *d_soln_time, double *d_dt,
                                           fvh_device_status *d_status,
                                           fvh_stream_t stream) {
-  if (!mesh || !state || !params || !d_soln_time || !d_dt || !d_status ||
-      (mesh->dim != 2 && mesh->dim != 3) || params->dim != mesh->dim ||
-      mesh->num_cells <= 0 || !mesh->cell_face_offsets || !mesh->cell_faces ||
-      !mesh->cell_volume || !mesh->face_area || !state->sound_speed ||
-      !(params->cfl > 0))
+  if (!fvh::mesh_ok(mesh) || !fvh::state_ok(state, mesh->dim) ||
+      !fvh::params_ok(params, mesh->dim) || !d_soln_time || !d_dt || !d_status)
     return FVH_ERR_INVALID_ARGUMENT;
-  for (int d = 0; d < mesh->dim; ++d)
-    if (!mesh->face_normal[d] || !state->velocity[d]) return FVH_ERR_INVALID_ARGUMENT;
   const long long nblocks =
       ((long long)mesh->num_cells + fvh::kDtThreads - 1) / fvh::kDtThreads;
   if (nblocks > kMaxBlocks) return FVH_ERR_CAPACITY;
@@ -84,7 +88,7 @@ fvh_status fvh_evaluate_time_step_noalloc(const fvh_mesh_view *mesh,
                                      (int)nblocks, d_status, s)
           : fvh::plain::launch_dt<3>(*mesh, *state, *params, d_soln_time, d_dt, partial,
                                      (int)nblocks, d_status, s);
-  return e == cudaSuccess ? FVH_OK : FVH_ERR_CUDA;
+  return fvh::from_cuda(e);
 }
 
 }  // extern "C"

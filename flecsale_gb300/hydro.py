@@ -305,7 +305,10 @@ class HostMesh:
     def _view(self, ptr, n, ctype) -> np.ndarray:
         # the ctypes array is the numpy base and holds a reference to the mesh,
         # so views outlive neither the arrays nor the mesh
-        buf = (ctype * max(n, 1)).from_address(C.cast(ptr, C.c_void_p).value)
+        addr = C.cast(ptr, C.c_void_p).value
+        if not addr:  # an empty list (a one-cell mesh has no neighbours)
+            return np.zeros(0, dtype=np.dtype(ctype))
+        buf = (ctype * max(n, 1)).from_address(addr)
         buf._owner = self
         return np.ctypeslib.as_array(buf)[:n]
 

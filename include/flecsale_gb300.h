@@ -505,10 +505,12 @@ fvh_status fvh_input_string(const fvh_input *in, const char *path, char *buf, si
 /* The keys inputs.h:112-132 reads: CFL, final_time, eos = {type = "ideal_gas",
  * gas_constant, specific_heat} into p (absent keys keep p's values), and
  * max_steps and output_freq into the counters (either may be null).  Another
- * eos type returns FVH_ERR_UNSUPPORTED (inputs.h:129-131).  Values out of range
- * (a non-positive or non-finite CFL, gamma <= 1, cv <= 0, a NaN final time, a
- * negative or fractional count) return FVH_ERR_INVALID_ARGUMENT and leave p and
- * the counters unchanged. */
+ * eos type returns FVH_ERR_UNSUPPORTED (inputs.h:129-131).  The merged
+ * parameters are validated, so the values p brings in for keys the file does
+ * not set must be valid too: a merged value out of range (a non-positive or
+ * non-finite CFL, gamma <= 1, cv <= 0, a NaN final time, a negative or
+ * fractional count) returns FVH_ERR_INVALID_ARGUMENT and leaves p and the
+ * counters unchanged.  fvh_params_default gives valid values. */
 fvh_status fvh_input_params(const fvh_input *in, fvh_params *p, int64_t *max_steps,
                             int64_t *output_freq);
 

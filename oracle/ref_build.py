@@ -2,8 +2,8 @@
 
 Recipe: g++ on oracle/ref_physics.cpp with -I <reference checkout> and the
 ristra stand-ins in oracle/ref_shim; no reference build system is used.  Only
-possible where the reference checkout exists (FLECSALE_REFERENCE, default
-/root/reference); elsewhere build_if_available() does nothing.
+possible where the reference checkout exists and the environment variable
+FLECSALE_REFERENCE names it; elsewhere build_if_available() does nothing.
 """
 from __future__ import annotations
 
@@ -16,12 +16,13 @@ LIB = os.path.join(OUT_DIR, "libref_physics.so")
 
 
 def reference_root() -> str:
-    return os.environ.get("FLECSALE_REFERENCE", "/root/reference")
+    """The reference checkout named by FLECSALE_REFERENCE ("" when unset)."""
+    return os.environ.get("FLECSALE_REFERENCE", "")
 
 
 def available() -> bool:
     r = reference_root()
-    return os.path.exists(os.path.join(r, "flecsale", "eqns", "euler_eqns.h"))
+    return bool(r) and os.path.exists(os.path.join(r, "flecsale", "eqns", "euler_eqns.h"))
 
 
 def build(force: bool = False) -> str:

@@ -10,8 +10,9 @@ import numpy as np
 import flecsale_gb300.hydro as H
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# the reference checkout, for the tests that also check against it when present
-REFERENCE = os.environ.get("FLECSALE_REFERENCE", "/root/reference")
+# the reference checkout named by FLECSALE_REFERENCE, for the tests that also
+# check against it; they skip when it is unset
+REFERENCE = os.environ.get("FLECSALE_REFERENCE", "")
 
 
 # ---------------------------------------------------------------------------

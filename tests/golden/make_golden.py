@@ -140,7 +140,9 @@ def make_physics_vectors(here: str) -> None:
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    os.environ.setdefault("FLECSALE_REFERENCE", ref)
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLECSALE_REFERENCE", "")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set FLECSALE_REFERENCE)")
+    os.environ["FLECSALE_REFERENCE"] = ref
     main(ref)
     make_physics_vectors(os.path.dirname(os.path.abspath(__file__)))

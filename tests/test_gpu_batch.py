@@ -172,3 +172,39 @@ def test_steps_split_across_calls_bitwise():
     assert np.all(c1 == 0) and np.all(c2 == 0) and np.array_equal(t1, t2)
     for k in range(len(meshes)):
         assert np.array_equal(b.get_state(k), one[k])
+
+
+def test_mismatched_carried_problem_is_refused_and_changes_nothing():
+    """A reassignment that carries a problem onto a mesh with a different cell
+    count is refused with FVH_ERR_INVALID_ARGUMENT before anything on the
+    device changes (host and device-side assignment): stepping on afterwards
+    gives the same bits as a batch that never saw the bad call."""
+    probs = _problems(3)
+    p = _params()
+    meshes = [m for m, _ in probs]
+
+    def fresh():
+        b = H.Batch.for_meshes(p, meshes, slack=2.0)
+        b.assign(meshes, 0.4, 10.0)
+        for k, (m, kind) in enumerate(probs):
+            b.set_state(k, H.initial_state(kind, m, p, seed=k), 0.0)
+        b.step(4)
+        return b
+
+    a, ref = fresh(), fresh()
+    other = H.HostMesh.box(2, (7, 5), [0, 0], [1, 1], 0.2, 9)
+    assert other.num_cells != meshes[0].num_cells
+    with pytest.raises(H.FvhError) as ei:
+        a.assign([other, meshes[1]], 0.4, 10.0, keep=[0, 1])
+    assert ei.value.code == H.ERR_INVALID_ARGUMENT
+    with pytest.raises(H.FvhError) as ei:
+        H.batch_assign_device(a, [H.DeviceMesh(other), H.DeviceMesh(meshes[1])], 0.4, 10.0,
+                              keep=[0, 1])
+    assert ei.value.code == H.ERR_INVALID_ARGUMENT
+    a.step(4)
+    ref.step(4)
+    ta, ca, _ = a.query()
+    tr, cr, _ = ref.query()
+    assert np.all(ca == 0) and np.array_equal(ta, tr)
+    for k in range(len(meshes)):
+        assert np.array_equal(a.get_state(k), ref.get_state(k))

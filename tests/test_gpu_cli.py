@@ -62,6 +62,30 @@ def test_cli_3d_box_mesh_matches_library_run(tmp_path):
 
 
 def test_cli_mixed_precision_option(tmp_path):
+    """--precision mixed --flux hllc: the dump read back is within relative L1
+    1e-4 (density and total energy, the mixed form's bar) of a library run of
+    the mixed form on the same input, and of the FP64 library run."""
     out = _run(["-f", os.path.join(INPUTS, "shock_box_3d_box.lua"), "--precision", "mixed",
                 "--flux", "hllc", "--output_dir", str(tmp_path)], str(tmp_path))
     assert "after 12 steps." in out
+    inp = H.Input(os.path.join(INPUTS, "shock_box_3d_box.lua"))
+    p64, max_steps, _ = inp.params(3)
+    mesh = inp.mesh()
+    got, t_cli, n_cli = H.read_dump(str(tmp_path / "shock_box_3d-solution_rank000000.txt"), 3,
+                                    mesh.num_cells, p64.gamma, p64.cv)
+    assert n_cli == 12
+    E = lambda s: s[0] * (s[4] + 0.5 * (s[1] ** 2 + s[2] ** 2 + s[3] ** 2))
+    l1 = lambda a, b: np.abs(a - b).sum() / np.abs(b).sum()
+    for precision in ("mixed", "fp64"):
+        p = H.Params.from_buffer_copy(p64)  # the input file's settings, as the driver reads them
+        p.flux_kind, p.precision = H.FLUX["hllc"], H.PRECISION[precision]
+        state = inp.initial_state(mesh, p)
+        dm, ds = H.DeviceMesh(mesh), H.DeviceState(3, mesh.num_cells)
+        s = H.Solver(dm, p)
+        ds.upload(state)
+        s.reset(0.0)
+        assert s.run(ds, max_steps) == 12
+        code, t, _ = s.status()
+        lib_run = ds.download()
+        assert code == 0 and abs(t - t_cli) <= 1e-4 * t
+        assert l1(got[0], lib_run[0]) <= 1e-4 and l1(E(got), E(lib_run)) <= 1e-4, precision

@@ -262,6 +262,63 @@ def test_full_size_four_quadrant_bitwise_and_conservative(cuda):
     assert np.array_equal(out, state)
 
 
+def _gpu_run(mesh, p, state, nsteps):
+    dmesh, dstate = H.DeviceMesh(mesh), H.DeviceState(mesh.dim, mesh.num_cells)
+    solver = H.Solver(dmesh, p)
+    dstate.upload(state)
+    solver.reset(0.0)
+    assert solver.run(dstate, nsteps) == nsteps
+    code, t, cell = solver.status()
+    assert code == 0, (code, cell)
+    return dstate.download(), t
+
+
+def _l1(a, b):
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def _energy(s, dim):
+    return s[0] * (s[1 + dim] + 0.5 * sum(s[1 + i] ** 2 for i in range(dim)))
+
+
+def test_benchmark_workload_200_steps_against_oracle(cuda):
+    """The benchmark workload at its own length: 1024^2 jittered (+-0.2h, seed
+    1) four-quadrant, HLLC, Barth-Jespersen, CFL 0.4, transmissive boundaries,
+    200 steps.  FP64 is bitwise equal to the oracle; the mixed form is within
+    relative L1 1e-4 of the oracle in density and total energy."""
+    mesh = H.HostMesh.box(2, (1024, 1024), [0, 0], [1, 1], 0.2, 1)
+    kw = dict(flux="hllc", cfl=0.4, final_time=1.0e9, boundary="outflow")
+    p = H.make_params(2, **kw)
+    s0 = H.initial_state("four_quadrant", mesh, p)
+    out, t_gpu = _gpu_run(mesh, p, s0, 200)
+    mix, t_mix = _gpu_run(mesh, H.make_params(2, precision="mixed", **kw), s0, 200)
+    O = __import__("oracle").load()
+    ref = s0.copy()
+    st, t, n = U.oracle_run(O, mesh, ref, p, 200)
+    assert st == 0 and n == 200 and t_gpu == t
+    assert np.array_equal(out, ref)
+    assert abs(t_mix - t) / t < 1e-4
+    assert _l1(mix[0], ref[0]) <= 1e-4 and _l1(_energy(mix, 2), _energy(ref, 2)) <= 1e-4
+
+
+def test_3d_shock_box_64cube_20_steps_against_oracle(cuda):
+    """The 3D shock box of the benchmark at 64^3 (262,144 hexes, jitter
+    +-0.15h, seed 2): inner cube, Rusanov, CFL 0.3, walls, 20 steps.  FP64
+    bitwise equal to the oracle; mixed within relative L1 1e-4."""
+    mesh = H.HostMesh.box(3, (64, 64, 64), [0, 0, 0], [1, 1, 1], 0.15, 2)
+    kw = dict(flux="rusanov", cfl=0.3, final_time=1.0e9)
+    p = H.make_params(3, **kw)
+    s0 = H.initial_state("inner_cube", mesh, p)
+    out, t_gpu = _gpu_run(mesh, p, s0, 20)
+    mix, _ = _gpu_run(mesh, H.make_params(3, precision="mixed", **kw), s0, 20)
+    O = __import__("oracle").load()
+    ref = s0.copy()
+    st, t, n = U.oracle_run(O, mesh, ref, p, 20)
+    assert st == 0 and n == 20 and t_gpu == t
+    assert np.array_equal(out, ref)
+    assert _l1(mix[0], ref[0]) <= 1e-4 and _l1(_energy(mix, 3), _energy(ref, 3)) <= 1e-4
+
+
 def test_deterministic_rerun(cuda):
     mesh = H.HostMesh.box(2, (96, 80), [0, 0], [1, 1], 0.2, 5)
     p = H.make_params(2, flux="hllc", cfl=0.4)

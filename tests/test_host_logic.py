@@ -87,6 +87,26 @@ def test_reference_arm_json_line():
     assert line["config"]["cells"] == 48 * 48
 
 
+def test_reference_arm_loads_no_product_code():
+    """The reference arm builds its mesh, initial state and parameters with the
+    oracle's own code: the process never imports the product package nor maps
+    its shared library."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', "
+            "'--warmup', '3', '--n', '32']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'libflecsale_gb300' not in maps, 'product library mapped'; "
+            "assert not [m for m in sys.modules if m.startswith('flecsale_gb300')], "
+            "'product package imported'; print('clean')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().endswith("clean")
+
+
 def test_binding_checks_plane_shapes_before_the_call():
     """The C ABI reads (and advance_host writes) all (5+dim) x num_cells
     doubles of a host state: the binding refuses smaller, larger, strided,

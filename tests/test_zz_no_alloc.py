@@ -7,9 +7,12 @@ must not pay cudaMalloc's implicit synchronisation.  Its scratch (the per-block
 partial maxima) is a fixed 64 KiB array inside the library, shared by all calls.
 
 The test calls it through the C ABI twice in a row, on two different states,
-and checks each result against fvh_evaluate_time_step with a caller workspace.
-The dt kernels are the bit-exact FP64 ones, so the tolerance is exact equality,
-as in the other dt parity tests.  This file is named to be collected last.
+and checks each result against fvh_evaluate_time_step with a caller workspace
+and against the oracle's evaluate_time_step.  The dt kernels are the bit-exact
+FP64 ones, so the tolerance is exact equality, as in the other dt parity tests.
+The 640x512 case needs more blocks (1,280) than fvh_evaluate_time_step launches
+(1,216, each striding over more cells), so the two entry points split the cells
+differently there.  This file is named to be collected last.
 """
 import ctypes as C
 
@@ -38,16 +41,17 @@ def _dt_noalloc(torch, L, mesh_view, sv, p, scal, status):
     return float(scal[1].item()), int(status.item())
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_noalloc_time_step_matches_workspace_version(cuda, dim):
+@pytest.mark.parametrize("dim,n", [(2, (300, 200)), (2, (640, 512)), (3, (30, 24, 20))])
+def test_noalloc_time_step_matches_workspace_version(cuda, dim, n):
     torch = cuda
     L = H.lib()
+    O = __import__("oracle").load()
     if dim == 2:
-        mesh = H.HostMesh.box(2, (300, 200), [0, 0], [1, 1], 0.2, 4)
+        mesh = H.HostMesh.box(2, n, [0, 0], [1, 1], 0.2, 4)
         p = H.make_params(2, flux="hllc", cfl=0.4, boundary="outflow")
         problems = ("four_quadrant", "kelvin_helmholtz")
     else:
-        mesh = H.HostMesh.box(3, (30, 24, 20), [0, 0, 0], [1, 1, 1], 0.15, 4)
+        mesh = H.HostMesh.box(3, n, [0, 0, 0], [1, 1, 1], 0.15, 4)
         p = H.make_params(3, flux="rusanov", cfl=0.3)
         problems = ("inner_cube", "kelvin_helmholtz")
     dmesh = H.DeviceMesh(mesh)
@@ -62,6 +66,8 @@ def test_noalloc_time_step_matches_workspace_version(cuda, dim):
         dt_new, st_new = _dt_noalloc(torch, L, dmesh.view, sv, p, scal, status)
         assert st_ref == -1 and st_new == -1
         assert dt_new == dt_ref and dt_new > 0
+        st_o, dt_o = U.oracle_time_step(O, mesh, state, p, 0.01)
+        assert st_o == 0 and dt_new == dt_o
 
 
 def test_noalloc_rejects_meshes_beyond_capacity(cuda):
