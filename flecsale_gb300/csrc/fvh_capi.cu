@@ -42,8 +42,8 @@ struct fvh_solver {
   fvh_gradient_view grads{};
   fvh_flux_view flux{};
   double *work = nullptr;          // gradients + fluxes
-  double *tables = nullptr;        // FP64 path: per-cell LSQ matrices, per-slot V/A
-  double *lsq = nullptr, *slot_dx = nullptr;
+  double *tables = nullptr;        // FP64 path: geometry-only tables (one allocation)
+  fvh::plain::tables tab;          // views into `tables`
   double *scalars = nullptr;       // [0] soln time, [1] dt, [2..] dt partials
   fvh_device_status *status = nullptr;
   double *host_scalars = nullptr;  // pinned: soln time
@@ -84,6 +84,7 @@ const char *fvh_status_string(int32_t s) {
     case FVH_ERR_NO_DEVICE: return "no CUDA device";
     case FVH_ERR_OUT_OF_MEMORY: return "out of device memory";
     case FVH_ERR_CAPACITY: return "request exceeds a fixed capacity";
+    case FVH_ERR_TIMEOUT: return "a kernel's bounded wait on its data copies ran out";
     default: return "unknown status";
   }
 }
@@ -236,17 +237,16 @@ fvh_status fvh_solver_create(const fvh_mesh_view *mesh, const fvh_params *params
         s->flux.energy = b;
       }
       // geometry-only tables (built once, same arithmetic as on the fly)
-      int32_t nnz = 0;
+      int32_t nnz[3] = {0, 0, 0};
+      const int32_t *offs[3] = {mesh->cell_face_offsets, mesh->cell_nbr_offsets,
+                                mesh->cell_vertex_offsets};
+      for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+        e = cudaMemcpy(&nnz[k], offs[k] + nc, sizeof(int32_t), cudaMemcpyDeviceToHost);
+      const size_t ntab = fvh::plain::table_doubles(D, nc, nf, nnz[0], nnz[1], nnz[2]);
+      if (e == cudaSuccess) e = cudaMalloc(&s->tables, sizeof(double) * ntab);
       if (e == cudaSuccess)
-        e = cudaMemcpy(&nnz, mesh->cell_face_offsets + nc, sizeof(int32_t), cudaMemcpyDeviceToHost);
-      const size_t nlsq = (size_t)fvh::plain::lsq_doubles_per_cell(D) * nc;
-      if (e == cudaSuccess) e = cudaMalloc(&s->tables, sizeof(double) * (nlsq + (size_t)nnz + 1));
-      if (e == cudaSuccess) {
-        s->lsq = s->tables;
-        s->slot_dx = s->tables + nlsq;
-        e = D == 2 ? fvh::plain::build_tables<2>(*mesh, s->lsq, s->slot_dx)
-                   : fvh::plain::build_tables<3>(*mesh, s->lsq, s->slot_dx);
-      }
+        e = D == 2 ? fvh::plain::build_tables<2>(*mesh, s->tables, nnz[0], nnz[1], nnz[2], &s->tab)
+                   : fvh::plain::build_tables<3>(*mesh, s->tables, nnz[0], nnz[1], nnz[2], &s->tab);
     } else {
       const fvh_status ms = fvh::mixed::create(*mesh, *params, &s->mixed);
       if (ms != FVH_OK) {
@@ -284,18 +284,21 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
   const int nb = dt_blocks(m.num_cells);
   fvh_status r = from_cuda(
-      m.dim == 2 ? fvh::plain::launch_dt<2>(m, *state, p, t, dt, partial, nb, s->status, st, s->slot_dx)
-                 : fvh::plain::launch_dt<3>(m, *state, p, t, dt, partial, nb, s->status, st, s->slot_dx));
+      m.dim == 2 ? fvh::plain::launch_dt<2>(m, *state, p, t, dt, partial, nb, s->status, st, s->tab.slot_dx)
+                 : fvh::plain::launch_dt<3>(m, *state, p, t, dt, partial, nb, s->status, st, s->tab.slot_dx));
   mark("dt");
   for (int stage = 0; stage < 2 && r == FVH_OK; ++stage) {
     if (p.order == 1)
       r = fvh_evaluate_gradients(&m, state, &s->grads, &p, fs);
     else
       r = from_cuda(m.dim == 2
-                        ? fvh::plain::launch_gradients<2>(m, *state, s->grads, p, st, s->lsq)
-                        : fvh::plain::launch_gradients<3>(m, *state, s->grads, p, st, s->lsq));
+                        ? fvh::plain::launch_gradients<2>(m, *state, s->grads, p, st, s->tab)
+                        : fvh::plain::launch_gradients<3>(m, *state, s->grads, p, st, s->tab));
     mark("gradients");
-    if (r == FVH_OK) r = fvh_evaluate_fluxes(&m, state, &s->grads, &s->flux, &p, fs);
+    if (r == FVH_OK)
+      r = from_cuda(m.dim == 2
+                        ? fvh::plain::launch_fluxes<2>(m, *state, s->grads, s->flux, p, st, s->tab)
+                        : fvh::plain::launch_fluxes<3>(m, *state, s->grads, s->flux, p, st, s->tab));
     mark("fluxes");
     if (r == FVH_OK) r = fvh_apply_update(&m, &p, dt, 0.5, &s->flux, state, t, s->status, fs);
     mark("update");
@@ -443,6 +446,13 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
   if (n < 0 || (n > 0 && (!x || !hi || !lo || !rn32 || !hi_as_double)))
     return FVH_ERR_INVALID_ARGUMENT;
   return from_cuda(fvh::mixed::debug_split(x, n, hi, lo, rn32, hi_as_double, cs(stream)));
+}
+
+fvh_status fvh_debug_sf64(int32_t op, const double *a, const double *b, int64_t n,
+                          double *out, fvh_stream_t stream) {
+  if (op < 0 || op > 9 || n < 0 || (n > 0 && (!a || !b || !out)))
+    return FVH_ERR_INVALID_ARGUMENT;
+  return from_cuda(fvh::plain::debug_sf64(op, a, b, n, out, cs(stream)));
 }
 
 int64_t fvh_solver_launches_per_run(const fvh_solver *s, int64_t nsteps) {

@@ -3,6 +3,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
+#include <cstdint>
+
 #include "flecsale_gb300.h"
 
 namespace fvh {
@@ -45,8 +48,24 @@ __device__ inline double block_max(double v) {
 #endif
 
 namespace plain {
-// slot_dx / lsq: optional per-mesh tables (null = compute on the fly; the
-// results are the same either way)
+// Geometry-only tables of the FP64 solver, built once per mesh with the same
+// operations the kernels would perform on the fly, so the results are the same
+// either way (a null member is computed on the fly).
+struct tables {
+  const double *lsq = nullptr;      // per cell: least-squares matrix terms, SoA planes
+  const double *slot_dx = nullptr;  // per (cell, face) slot: V_c / A_f
+  const double *nbr_dx = nullptr;   // per (cell, neighbour) slot: x_nbr - x_c, D doubles
+  const double *vtx_dx = nullptr;   // per (cell, vertex) slot: x_v - x_c, D doubles
+  const double *face_dx = nullptr;  // per face: x_f - x_c0 then x_f - x_c1, 2D doubles
+};
+// doubles the tables of a mesh take (nnz_*: the CSR list lengths)
+size_t table_doubles(int dim, int64_t nc, int64_t nf, int64_t nnz_cf, int64_t nnz_nb,
+                     int64_t nnz_cv);
+// carves the tables out of `base` (table_doubles long) and fills them
+template <int D>
+cudaError_t build_tables(const fvh_mesh_view &m, double *base, int64_t nnz_cf,
+                         int64_t nnz_nb, int64_t nnz_cv, tables *t);
+
 template <int D>
 cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
                       const fvh_params &p, const double *soln_time, double *dt,
@@ -55,14 +74,16 @@ cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
 template <int D>
 cudaError_t launch_gradients(const fvh_mesh_view &m, const fvh_state_view &s,
                              const fvh_gradient_view &g, const fvh_params &p,
-                             cudaStream_t st, const double *lsq = nullptr);
-template <int D>
-cudaError_t build_tables(const fvh_mesh_view &m, double *lsq, double *slot_dx);
-int lsq_doubles_per_cell(int dim);
+                             cudaStream_t st, const tables &t = tables());
 template <int D>
 cudaError_t launch_fluxes(const fvh_mesh_view &m, const fvh_state_view &s,
                           const fvh_gradient_view &g, const fvh_flux_view &fl,
-                          const fvh_params &p, cudaStream_t st);
+                          const fvh_params &p, cudaStream_t st, const tables &t = tables());
+// Diagnostic: out[i] = a[i] op b[i] for op 0 mul, 1 add, 2 sub, 3 div on the
+// integer pipes (fvh_sf64.cuh), 4..7 the same with the FP64 instructions,
+// 8 / 9 the optimistic mul / div with their FP64 redo.
+cudaError_t debug_sf64(int op, const double *a, const double *b, int64_t n, double *out,
+                       cudaStream_t st);
 template <int D>
 cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const double *dt,
                           double factor, const fvh_flux_view &fl,

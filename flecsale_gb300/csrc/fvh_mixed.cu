@@ -31,6 +31,7 @@
 // conservative to double-float rounding without atomics.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <new>
 #include <vector>
@@ -38,6 +39,7 @@
 #include "fvh_kernels.h"
 #include "fvh_mixed.h"
 #include "fvh_physics.cuh"
+#include "fvh_tma.cuh"
 
 namespace fvh {
 namespace mixed {
@@ -59,6 +61,23 @@ struct layout {
   static constexpr int FDX4 = D == 2 ? 1 : 2;  // x_f - x_c0, x_f - x_c1
   static constexpr int FLUX4 = D == 2 ? 1 : 2; // face flux (D+2 floats, padded)
   static constexpr int DEL4 = D == 2 ? 2 : 3;  // predictor increments (D+2 double-floats)
+};
+
+// Staged 2D gradients (gradients_staged_kernel).  A chunk is a set of up to
+// kStageCells cells; its staged records are listed as runs of consecutive ids:
+// ids [first, first + count) go to positions [slot, slot + count); kind 0 =
+// cells (pack + centroid), 1 = vertices.
+struct stage_run {
+  int first, count, slot, kind;
+};
+
+struct stage_tables {
+  int nchunks = 0;
+  const int *cells = nullptr;                // [nchunks * kStageCells] cell ids, -1 = none
+  const int *run_off = nullptr;              // [nchunks + 1] into runs
+  const stage_run *runs = nullptr;
+  const long long *topo_off = nullptr;       // [nchunks + 1] byte offsets into topo
+  const unsigned short *topo = nullptr;      // per chunk: see setup_stage_host
 };
 
 struct workspace {
@@ -83,6 +102,11 @@ struct workspace {
   float *acc = nullptr;
   int ncolours = 0;
   int colour_off[kMaxColours + 1] = {};
+  // staged 2D gradients (single mesh, when every chunk fits); stage_base owns
+  // the tables' device memory
+  stage_tables stage;
+  void *stage_base = nullptr;
+  int stage_blocks = 0;  // persistent grid
 };
 
 __device__ __forceinline__ void stg256(float4 *p, float4 a, float4 b) {
@@ -689,10 +713,10 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 // centroid.  2D gradients 56.4 -> 54.6 us at 1024^2; in 3D the pairs keep more
 // registers live in a kernel already at 96 and measured 3.6 % slower per step,
 // so 3D takes the scalar form above.
-template <int D, bool LIMIT, int UNROLL, class NBR>
-__device__ __forceinline__ void cell_gradients_pairs(const fvh_mesh_view &m, const workspace &w,
-                                                     int c0, float4 a0, float4 b0, const float *xh,
-                                                     const float *xl, int nn, NBR nbr) {
+template <int D, bool LIMIT, int UNROLL, class NBR, class VTX>
+__device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0, float4 a0,
+                                                     float4 b0, const float *xh, const float *xl,
+                                                     int nn, NBR nbr, int nr, VTX vtx) {
   constexpr int NV = D + 4;       // values (slots 0 .. NV-1 of the pack)
   constexpr int NP = NV / 2;      // slot pairs; 3D has slot NV-1 (a) left over
   constexpr bool ODD = NV % 2 == 1;
@@ -795,10 +819,9 @@ __device__ __forceinline__ void cell_gradients_pairs(const fvh_mesh_view &m, con
     float dpos[NV], dneg[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) dpos[k] = dneg[k] = 0.f;
-    const int r0 = m.cell_vertex_offsets[c0], nr = m.cell_vertex_offsets[c0 + 1] - r0;
     for (int r = 0; r < nr; ++r) {
       float vh[3], vl[3], dxv[3];
-      load_cen<D>(w.vcoord, m.cell_vertices[r0 + r], vh, vl);
+      vtx(r, vh, vl);
 #pragma unroll
       for (int i = 0; i < D; ++i) dxv[i] = __fadd_rn(__fsub_rn(vh[i], xh[i]), __fsub_rn(vl[i], xl[i]));
 #pragma unroll
@@ -877,12 +900,15 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
     if (D == 2) {
       float4 a0, b0;
       ldg256(pk + 2 * (size_t)c0, a0, b0);
-      cell_gradients_pairs<D, LIMIT, 4>(m, w, c0, a0, b0, xh, xl, nn,
-                                        [&](int q, float4 &a, float4 &b, float *yh, float *yl) {
-                                          const int c1 = m.cell_nbrs[q0 + q];
-                                          ldg256(pk + 2 * (size_t)c1, a, b);
-                                          load_cen<D>(w.ccen, c1, yh, yl);
-                                        });
+      const int r0 = m.cell_vertex_offsets[c0], nr = m.cell_vertex_offsets[c0 + 1] - r0;
+      cell_gradients_pairs<D, LIMIT, 4>(
+          w, c0, a0, b0, xh, xl, nn,
+          [&](int q, float4 &a, float4 &b, float *yh, float *yl) {
+            const int c1 = m.cell_nbrs[q0 + q];
+            ldg256(pk + 2 * (size_t)c1, a, b);
+            load_cen<D>(w.ccen, c1, yh, yl);
+          },
+          nr, [&](int r, float *vh, float *vl) { load_cen<D>(w.vcoord, m.cell_vertices[r0 + r], vh, vl); });
     } else {
       float u0[D + 4];
       pack_values<D>(load_pack<D>(pk, c0), u0);
@@ -893,6 +919,142 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
                                     load_cen<D>(w.ccen, c1, yh, yl);
                                   });
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2D gradients from records staged in shared memory by the bulk-copy (TMA)
+// engine
+// ---------------------------------------------------------------------------
+// The gathers of gradients_kernel are dependent loads (offsets -> neighbour
+// ids -> records) that keep it latency-bound.  Here the cells are taken in
+// chunks of up to kStageCells cells that lie close together (consecutive in
+// the Morton order of the cell centroids: a compact tile of a box), one cell
+// per thread.  A chunk reads the pack and centroid of a set of cells (its own
+// and their vertex neighbours) and the coordinates of its cells' vertices; on
+// a mesh numbered row by row these sets are a few runs of consecutive ids.  The
+// setup lists each chunk's runs and packs, per cell, its own record's position
+// and those of its neighbours and vertices in the chunk's staged set (16 bits
+// each).  A persistent kernel posts the copies of chunk i+1 (one bulk copy per
+// run and array, plus one for the chunk's topology; completion counted on an
+// mbarrier) while its threads compute chunk i from shared memory with the
+// arithmetic of gradients_kernel (cell_gradients_pairs), so both kernels give
+// the same bits.
+constexpr int kStageCells = 128;     // cells per chunk = threads per block
+constexpr int kStageMaxCells = 256;  // staged cell records per chunk
+constexpr int kStageMaxVerts = 224;  // staged vertex records per chunk
+constexpr int kStageTopoBytes = 5120;
+constexpr int kStagePackBytes = kStageMaxCells * 32;
+constexpr int kStageCenBytes = kStageMaxCells * 16;
+constexpr int kStageVtxBytes = kStageMaxVerts * 16;
+constexpr int kStageBytes = kStagePackBytes + kStageCenBytes + kStageVtxBytes + kStageTopoBytes;
+constexpr int kStageWaitPolls = 1 << 22;  // bounded waits on a chunk's copies
+
+template <bool LIMIT>
+__global__ void __launch_bounds__(kStageCells)
+gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ pk,
+                        stage_tables t, int rev, fvh_device_status *status) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long bar[2];
+  const int tid = threadIdx.x;
+  auto chunk_at = [&](int i) { return rev ? t.nchunks - 1 - i : i; };
+  // posts the copies of chunk k into stage buffer b (warp 0)
+  auto post = [&](int k, int b) {
+    const int r0 = t.run_off[k], nr = t.run_off[k + 1] - r0;
+    const long long tb0 = t.topo_off[k];
+    const unsigned topo_bytes = (unsigned)(t.topo_off[k + 1] - tb0);
+    unsigned char *base = smem + (size_t)b * kStageBytes;
+    // this buffer's earlier reads (ordered by the block barrier) come before
+    // the copies that overwrite it
+    tma::fence_proxy_async_shared();
+    if (tid == 0) {
+      unsigned bytes = topo_bytes;
+      for (int r = 0; r < nr; ++r) {
+        const stage_run run = t.runs[r0 + r];
+        bytes += (unsigned)run.count * (run.kind == 0 ? 48u : 16u);
+      }
+      tma::mbar_arrive_expect_tx(&bar[b], bytes);
+      tma::bulk_g2s(base + kStagePackBytes + kStageCenBytes + kStageVtxBytes,
+                    reinterpret_cast<const unsigned char *>(t.topo) + tb0, topo_bytes, &bar[b]);
+    }
+    __syncwarp();
+    for (int r = tid; r < nr; r += 32) {
+      const stage_run run = t.runs[r0 + r];
+      if (run.kind == 0) {
+        tma::bulk_g2s(base + (size_t)run.slot * 32, pk + 2 * (size_t)run.first,
+                      (unsigned)run.count * 32u, &bar[b]);
+        tma::bulk_g2s(base + kStagePackBytes + (size_t)run.slot * 16, w.ccen + run.first,
+                      (unsigned)run.count * 16u, &bar[b]);
+      } else {
+        tma::bulk_g2s(base + kStagePackBytes + kStageCenBytes + (size_t)run.slot * 16,
+                      w.vcoord + run.first, (unsigned)run.count * 16u, &bar[b]);
+      }
+    }
+  };
+  if (tid == 0) {
+    tma::mbar_init(&bar[0], 1);
+    tma::mbar_init(&bar[1], 1);
+    tma::fence_barrier_init();
+  }
+  __syncthreads();
+  // copies posted into / phases consumed from each buffer (the same in every
+  // thread: the decisions below are uniform across the block)
+  int posted[2] = {0, 0}, used[2] = {0, 0};
+  if ((int)blockIdx.x < t.nchunks) {
+    if (tid < 32) post(chunk_at(blockIdx.x), 0);
+    posted[0] = 1;
+  }
+  int it = 0;
+  for (int i = blockIdx.x; i < t.nchunks; i += gridDim.x, ++it) {
+    const int b = it & 1;
+    // the other buffer was last read by the previous chunk, before the
+    // barrier that ended it
+    if (i + (int)gridDim.x < t.nchunks) {
+      if (tid < 32) post(chunk_at(i + gridDim.x), b ^ 1);
+      ++posted[b ^ 1];
+    }
+    const int k = chunk_at(i);
+    const int c0 = t.cells[(size_t)k * kStageCells + tid];
+    const bool landed = tma::mbar_wait_bounded(&bar[b], (unsigned)(used[b] & 1), kStageWaitPolls);
+    if (__syncthreads_or(!landed)) {
+      // report, then wait (bounded) for every posted copy before leaving, so
+      // none lands in shared memory this block no longer owns
+      if (tid == 0) atomicMin(status, status_key(t.cells[(size_t)k * kStageCells], FVH_ERR_TIMEOUT));
+      for (int bb = 0; bb < 2; ++bb)
+        if (posted[bb] > used[bb])
+          tma::mbar_wait_bounded(&bar[bb], (unsigned)((posted[bb] - 1) & 1), kStageWaitPolls);
+      return;
+    }
+    ++used[b];
+    const unsigned char *base = smem + (size_t)b * kStageBytes;
+    const float4 *spk = reinterpret_cast<const float4 *>(base);
+    const float4 *scen = reinterpret_cast<const float4 *>(base + kStagePackBytes);
+    const float4 *svtx = reinterpret_cast<const float4 *>(base + kStagePackBytes + kStageCenBytes);
+    const unsigned short *topo = reinterpret_cast<const unsigned short *>(
+        base + kStagePackBytes + kStageCenBytes + kStageVtxBytes);
+    if (c0 >= 0) {
+      const unsigned short *rec = topo + topo[tid];
+      const int own = rec[0], nn = rec[1], nr = rec[2];
+      const unsigned short *nslot = rec + 3, *vslot = rec + 3 + nn;
+      const float4 a0 = spk[2 * own], b0 = spk[2 * own + 1];
+      const float4 x0 = scen[own];
+      const float xh[3] = {x0.x, x0.y, 0.f}, xl[3] = {x0.z, x0.w, 0.f};
+      cell_gradients_pairs<2, LIMIT, 4>(
+          w, c0, a0, b0, xh, xl, nn,
+          [&](int q, float4 &a, float4 &bb, float *yh, float *yl) {
+            const int sl = nslot[q];
+            a = spk[2 * sl];
+            bb = spk[2 * sl + 1];
+            const float4 y = scen[sl];
+            yh[0] = y.x; yh[1] = y.y; yl[0] = y.z; yl[1] = y.w;
+          },
+          nr,
+          [&](int r, float *vh, float *vl) {
+            const float4 v = svtx[vslot[r]];
+            vh[0] = v.x; vh[1] = v.y; vl[0] = v.z; vl[1] = v.w;
+          });
+    }
+    __syncthreads();
   }
 }
 
@@ -1521,12 +1683,182 @@ static cudaError_t setup_colours_host(workspace *w, const fvh_mesh_view &m) {
 
 int colours(const workspace *w) { return w ? w->ncolours : 0; }
 
+// Tables of the staged 2D gradients (see gradients_staged_kernel), built on
+// the host from the mesh.  Chunks: kStageCells consecutive cells of the Morton
+// order of the centroids (16-bit quantised coordinates, bits interleaved).
+// Per chunk, a topology block of 16-bit words: word i (i < kStageCells) is the
+// start of cell i's record (or 0xffff), a record is (own slot, number of
+// neighbours nn, number of vertices nr, nn neighbour slots, nr vertex slots);
+// the block is padded to 16 bytes.  A mesh with a chunk whose staged set or
+// topology does not fit keeps the global-memory kernel (nchunks stays 0).
+static unsigned spread_bits16(unsigned x) {
+  x &= 0xffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
+  const int nc = m.num_cells;
+  std::vector<int> nb_off(nc + 1), cv_off(nc + 1);
+  std::vector<double> cx(nc), cy(nc);
+  cudaError_t e = cudaMemcpy(nb_off.data(), m.cell_nbr_offsets, sizeof(int) * (nc + 1),
+                             cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(cv_off.data(), m.cell_vertex_offsets, sizeof(int) * (nc + 1),
+                   cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(cx.data(), m.cell_centroid[0], sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(cy.data(), m.cell_centroid[1], sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  std::vector<int> nb(nb_off[nc]), cv(cv_off[nc]);
+  if (!nb.empty())
+    e = cudaMemcpy(nb.data(), m.cell_nbrs, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && !cv.empty())
+    e = cudaMemcpy(cv.data(), m.cell_vertices, sizeof(int) * cv.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  // Morton order of the centroids
+  double x0 = cx[0], x1 = cx[0], y0 = cy[0], y1 = cy[0];
+  for (int c = 0; c < nc; ++c) {
+    x0 = std::min(x0, cx[c]); x1 = std::max(x1, cx[c]);
+    y0 = std::min(y0, cy[c]); y1 = std::max(y1, cy[c]);
+  }
+  const double sx = x1 > x0 ? 65535.0 / (x1 - x0) : 0.0, sy = y1 > y0 ? 65535.0 / (y1 - y0) : 0.0;
+  std::vector<std::pair<unsigned, int>> order(nc);
+  for (int c = 0; c < nc; ++c) {
+    const unsigned qx = (unsigned)((cx[c] - x0) * sx), qy = (unsigned)((cy[c] - y0) * sy);
+    order[c] = {spread_bits16(qx) | (spread_bits16(qy) << 1), c};
+  }
+  std::sort(order.begin(), order.end());
+  const int nchunks = (nc + kStageCells - 1) / kStageCells;
+  std::vector<std::vector<stage_run>> runs(nchunks);
+  std::vector<std::vector<unsigned short>> topo(nchunks);
+  int fits = 1;
+#pragma omp parallel for schedule(dynamic, 16) reduction(& : fits)
+  for (int k = 0; k < nchunks; ++k) {
+    const int i0 = k * kStageCells, i1 = std::min(nc, i0 + kStageCells);
+    std::vector<int> ids, vids;
+    for (int i = i0; i < i1; ++i) {
+      const int c = order[i].second;
+      ids.push_back(c);
+      for (int q = nb_off[c]; q < nb_off[c + 1]; ++q) ids.push_back(nb[q]);
+      for (int r = cv_off[c]; r < cv_off[c + 1]; ++r) vids.push_back(cv[r]);
+    }
+    std::sort(ids.begin(), ids.end());
+    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+    std::sort(vids.begin(), vids.end());
+    vids.erase(std::unique(vids.begin(), vids.end()), vids.end());
+    if ((int)ids.size() > kStageMaxCells || (int)vids.size() > kStageMaxVerts) {
+      fits = 0;
+      continue;
+    }
+    auto add_runs = [&](const std::vector<int> &v, int kind) {
+      for (size_t i = 0; i < v.size();) {
+        size_t j = i + 1;
+        while (j < v.size() && v[j] == v[j - 1] + 1) ++j;
+        runs[k].push_back({v[i], (int)(j - i), (int)i, kind});
+        i = j;
+      }
+    };
+    add_runs(ids, 0);
+    add_runs(vids, 1);
+    auto pos = [](const std::vector<int> &v, int x) {
+      return (unsigned short)(std::lower_bound(v.begin(), v.end(), x) - v.begin());
+    };
+    std::vector<unsigned short> &tb = topo[k];
+    tb.assign(kStageCells, 0xffffu);
+    for (int i = i0; i < i1; ++i) {
+      const int c = order[i].second;
+      tb[i - i0] = (unsigned short)tb.size();
+      tb.push_back(pos(ids, c));
+      tb.push_back((unsigned short)(nb_off[c + 1] - nb_off[c]));
+      tb.push_back((unsigned short)(cv_off[c + 1] - cv_off[c]));
+      for (int q = nb_off[c]; q < nb_off[c + 1]; ++q) tb.push_back(pos(ids, nb[q]));
+      for (int r = cv_off[c]; r < cv_off[c + 1]; ++r) tb.push_back(pos(vids, cv[r]));
+      if (tb.size() > 0xffffu) break;
+    }
+    while (tb.size() % 8) tb.push_back(0);  // 16-byte multiple
+    if (tb.size() * 2 > (size_t)kStageTopoBytes) fits = 0;
+  }
+  if (!fits) return cudaSuccess;  // the global-memory kernel serves this mesh
+  std::vector<int> cells((size_t)nchunks * kStageCells, -1);
+  for (int i = 0; i < nc; ++i) cells[i] = order[i].second;
+  std::vector<int> run_off(nchunks + 1, 0);
+  std::vector<long long> topo_off(nchunks + 1, 0);
+  for (int k = 0; k < nchunks; ++k) {
+    run_off[k + 1] = run_off[k] + (int)runs[k].size();
+    topo_off[k + 1] = topo_off[k] + 2 * (long long)topo[k].size();
+  }
+  std::vector<stage_run> all(run_off[nchunks]);
+  std::vector<unsigned short> blob(topo_off[nchunks] / 2);
+  for (int k = 0; k < nchunks; ++k) {
+    std::copy(runs[k].begin(), runs[k].end(), all.begin() + run_off[k]);
+    std::copy(topo[k].begin(), topo[k].end(), blob.begin() + topo_off[k] / 2);
+  }
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t b_cells = up(sizeof(int) * cells.size()), b_off = up(sizeof(int) * run_off.size()),
+               b_runs = up(sizeof(stage_run) * all.size()),
+               b_toff = up(sizeof(long long) * topo_off.size()),
+               b_topo = up(sizeof(unsigned short) * blob.size());
+  char *base = nullptr;
+  e = cudaMalloc(&base, b_cells + b_off + b_runs + b_toff + b_topo);
+  if (e != cudaSuccess) return e;
+  w->stage_base = base;
+  char *p = base;
+  auto put = [&](const void *src, size_t bytes, size_t span) {
+    char *d = p;
+    if (e == cudaSuccess && bytes) e = cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice);
+    p += span;
+    return d;
+  };
+  stage_tables t;
+  t.nchunks = nchunks;
+  t.cells = reinterpret_cast<const int *>(put(cells.data(), sizeof(int) * cells.size(), b_cells));
+  t.run_off = reinterpret_cast<const int *>(put(run_off.data(), sizeof(int) * run_off.size(), b_off));
+  t.runs = reinterpret_cast<const stage_run *>(put(all.data(), sizeof(stage_run) * all.size(), b_runs));
+  t.topo_off = reinterpret_cast<const long long *>(
+      put(topo_off.data(), sizeof(long long) * topo_off.size(), b_toff));
+  t.topo = reinterpret_cast<const unsigned short *>(
+      put(blob.data(), sizeof(unsigned short) * blob.size(), b_topo));
+  if (e != cudaSuccess) return e;
+  // persistent grid: the blocks that fit on the device at once
+  const int smem = 2 * kStageBytes;
+  e = cudaFuncSetAttribute(gradients_staged_kernel<true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(gradients_staged_kernel<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int per_sm = 0, dev = 0, sms = 0;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradients_staged_kernel<true>,
+                                                      kStageCells, smem);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess || per_sm < 1) return e;
+  w->stage = t;
+  w->stage_blocks = std::min(nchunks, per_sm * sms);
+  return cudaSuccess;
+}
+
+static cudaError_t setup_stage(workspace *w, const fvh_mesh_view &m) {
+  if (m.dim != 2) return cudaSuccess;
+  try {
+    return setup_stage_host(w, m);
+  } catch (const std::bad_alloc &) {
+    return cudaErrorMemoryAllocation;
+  }
+}
+
 fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) {
   (void)p;
   const fvh_status r = create_capacity(m.dim, m.num_cells, m.num_faces, m.num_vertices, out);
   if (r != FVH_OK) return r;
   cudaError_t e = setup_geometry(*out, m, nullptr);
   if (e == cudaSuccess) e = setup_colours(*out, m);
+  if (e == cudaSuccess) e = setup_stage(*out, m);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     destroy(*out);
@@ -1538,6 +1870,7 @@ fvh_status create(const fvh_mesh_view &m, const fvh_params &p, workspace **out) 
 
 void destroy(workspace *w) {
   if (!w) return;
+  cudaFree(w->stage_base);
   cudaFree(w->colour_faces);
   cudaFree(w->acc);
   cudaFree(w->base);
@@ -1564,10 +1897,19 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
   const int nb_next = nb < kCflMaxBlocks ? nb : kCflMaxBlocks;
   if (SECOND) {
     dir ^= 1;
-    if (p.limiter == FVH_LIMITER_NONE)
+    if (D == 2 && w->stage.nchunks > 0 && !pm.cell_problem) {
+      const int smem = 2 * kStageBytes;
+      if (p.limiter == FVH_LIMITER_NONE)
+        gradients_staged_kernel<false><<<w->stage_blocks, kStageCells, smem, st>>>(
+            m, *w, pk_in, w->stage, dir, pm.status);
+      else
+        gradients_staged_kernel<true><<<w->stage_blocks, kStageCells, smem, st>>>(
+            m, *w, pk_in, w->stage, dir, pm.status);
+    } else if (p.limiter == FVH_LIMITER_NONE) {
       gradients_kernel<D, false, BS><<<nb, BS, 0, st>>>(m, *w, pk_in, dir);
-    else
+    } else {
       gradients_kernel<D, true, BS><<<nb, BS, 0, st>>>(m, *w, pk_in, dir);
+    }
     mark("gradients");
   }
   update_consts k;

@@ -16,25 +16,104 @@
 // gathers follow the CSR lists in the reference's iteration order; with
 // lexicographic numbering the neighbours of a warp's cells share cache lines and
 // are served from L1/L2 after the first touch.
+//
+// Pipes: GB300 issues 2 FP64 operations per clock per SM.  Every product and
+// quotient below is computed on the integer/FP32 pipes by the correctly
+// rounded routines of fvh_sf64.cuh, while sums and differences stay on the
+// FP64 pipe; comparisons, minima and maxima run on integer order keys.  Both
+// pipes round to nearest-even exactly as IEEE binary64 does, so the bits are
+// unchanged, and they work at the same time.  Each unit of work (a cell or a
+// face) is evaluated optimistically with the branch-free integer forms
+// (arith_opt); if any operand was of a kind they do not handle (subnormal,
+// infinite, NaN, beyond 2^+-500) the unit is evaluated again with the FP64
+// instructions (arith_hw) and that result is kept.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
 #include "flecsale_gb300.h"
 #include "fvh_kernels.h"
+#include "fvh_sf64.cuh"
 
 namespace fvh {
 namespace plain {
 
-// std::max / std::min semantics of the reference (a < b ? b : a)
-__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+// Products and quotients of one unit of work: on the integer pipes, noting
+// any operand they leave to the hardware ...
+struct arith_opt {
+  unsigned rare = 0;
+  __device__ __forceinline__ double mul(double a, double b) { return sf64::mul_opt(a, b, rare); }
+  __device__ __forceinline__ double quo(double a, double b) { return sf64::div_opt(a, b, rare); }
+};
+// ... and with the FP64 instructions (the evaluation kept when `rare`)
+struct arith_hw {
+  __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  __device__ __forceinline__ double quo(double a, double b) { return __ddiv_rn(a, b); }
+};
 
-template <int D>
-__device__ __forceinline__ double dot(const double *a, const double *b) {
+// IEEE comparisons decided on the integer pipe (an FP64 compare would take an
+// FP64 issue slot): order keys of the two's-complement kind, NaN unordered.
+__device__ __forceinline__ bool is_nan(unsigned lo, unsigned hi) {
+  const unsigned h = hi & 0x7fffffffu;
+  return h > 0x7ff00000u || (h == 0x7ff00000u && lo != 0u);
+}
+__device__ __forceinline__ long long cmp_key(unsigned lo, unsigned hi) {
+  // -0 and +0 share a key; a < b exactly when key(a) < key(b) for non-NaN
+  long long b = (long long)(((unsigned long long)hi << 32) | lo);
+  b = (b == (long long)0x8000000000000000ull) ? 0ll : b;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+// a < b
+__device__ __forceinline__ bool lt(double a, double b) {
+  unsigned al, ah, bl, bh;
+  sf64::halves(a, al, ah);
+  sf64::halves(b, bl, bh);
+  return !is_nan(al, ah) && !is_nan(bl, bh) && cmp_key(al, ah) < cmp_key(bl, bh);
+}
+// x >= 0, x <= 0, x < 0
+__device__ __forceinline__ bool ge0(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return !is_nan(lo, hi) && ((hi >> 31) == 0u || sf64::is_zero(lo, hi));
+}
+__device__ __forceinline__ bool le0(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return !is_nan(lo, hi) && ((hi >> 31) != 0u || sf64::is_zero(lo, hi));
+}
+__device__ __forceinline__ bool lt0(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return !is_nan(lo, hi) && (hi >> 31) != 0u && !sf64::is_zero(lo, hi);
+}
+// x == +-0
+__device__ __forceinline__ bool is_zero(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return sf64::is_zero(lo, hi);
+}
+// neither -0 nor a NaN (x + (+-0) == x bit for bit)
+__device__ __forceinline__ bool ordinary(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return !is_nan(lo, hi) && !(hi == 0x80000000u && lo == 0u);
+}
+// |x| by clearing the sign bit
+__device__ __forceinline__ double absval(double x) {
+  unsigned lo, hi;
+  sf64::halves(x, lo, hi);
+  return sf64::join(lo, hi & 0x7fffffffu);
+}
+
+// std::max / std::min semantics of the reference (a < b ? b : a)
+__device__ __forceinline__ double smax(double a, double b) { return lt(a, b) ? b : a; }
+__device__ __forceinline__ double smin(double a, double b) { return lt(b, a) ? b : a; }
+
+template <int D, class A>
+__device__ __forceinline__ double dot(A &ar, const double *a, const double *b) {
   double s = 0;
 #pragma unroll
-  for (int i = 0; i < D; ++i) s += a[i] * b[i];
+  for (int i = 0; i < D; ++i) s += ar.mul(a[i], b[i]);
   return s;
 }
 
@@ -45,113 +124,114 @@ struct prim {
   double d, v[D], p, e, a;
 };
 
-template <int D>
-__device__ __forceinline__ double total_energy(const prim<D> &u) {
-  return u.e + 0.5 * dot<D>(u.v, u.v);
+template <int D, class A>
+__device__ __forceinline__ double total_energy(A &ar, const prim<D> &u) {
+  return u.e + ar.mul(0.5, dot<D>(ar, u.v, u.v));
 }
 
-template <int D>
-__device__ __forceinline__ void phys_flux(const prim<D> &u, const double *n, double *f) {
-  const double et = total_energy<D>(u);
-  const double vn = dot<D>(u.v, n);
-  const double mass_flux = u.d * vn;
+template <int D, class A>
+__device__ __forceinline__ void phys_flux(A &ar, const prim<D> &u, const double *n, double *f) {
+  const double et = total_energy<D>(ar, u);
+  const double vn = dot<D>(ar, u.v, n);
+  const double mass_flux = ar.mul(u.d, vn);
   f[0] = mass_flux;
 #pragma unroll
-  for (int i = 0; i < D; ++i) f[1 + i] = mass_flux * u.v[i] + u.p * n[i];
-  f[D + 1] = mass_flux * (et + u.p / u.d);
+  for (int i = 0; i < D; ++i) f[1 + i] = ar.mul(mass_flux, u.v[i]) + ar.mul(u.p, n[i]);
+  f[D + 1] = ar.mul(mass_flux, et + ar.quo(u.p, u.d));
 }
 
-template <int D>
-__device__ __forceinline__ void solution_delta(const prim<D> &l, const prim<D> &r,
+template <int D, class A>
+__device__ __forceinline__ void solution_delta(A &ar, const prim<D> &l, const prim<D> &r,
                                                double *du) {
-  const double ener_l = l.d * total_energy<D>(l);
-  const double ener_r = r.d * total_energy<D>(r);
+  const double ener_l = ar.mul(l.d, total_energy<D>(ar, l));
+  const double ener_r = ar.mul(r.d, total_energy<D>(ar, r));
   du[0] = r.d - l.d;
 #pragma unroll
-  for (int i = 0; i < D; ++i) du[1 + i] = r.d * r.v[i] - l.d * l.v[i];
+  for (int i = 0; i < D; ++i) du[1 + i] = ar.mul(r.d, r.v[i]) - ar.mul(l.d, l.v[i]);
   du[D + 1] = ener_r - ener_l;
 }
 
-template <int D>
-__device__ __forceinline__ void hlle(const prim<D> &l, const prim<D> &r,
+template <int D, class A>
+__device__ __forceinline__ void hlle(A &ar, const prim<D> &l, const prim<D> &r,
                                      const double *n, double *f) {
-  const double vnl = dot<D>(l.v, n), vnr = dot<D>(r.v, n);
+  const double vnl = dot<D>(ar, l.v, n), vnr = dot<D>(ar, r.v, n);
   const double lambda_l = smin(vnl - l.a, vnr - r.a);
   const double lambda_r = smax(vnl + l.a, vnr + r.a);
-  if (lambda_l >= 0) {
-    phys_flux<D>(l, n, f);
-  } else if (lambda_r <= 0) {
-    phys_flux<D>(r, n, f);
+  if (ge0(lambda_l)) {
+    phys_flux<D>(ar, l, n, f);
+  } else if (le0(lambda_r)) {
+    phys_flux<D>(ar, r, n, f);
   } else {
     double fl[D + 2], fr[D + 2], du[D + 2];
-    phys_flux<D>(l, n, fl);
-    phys_flux<D>(r, n, fr);
-    const double c1 = lambda_l * lambda_r;
+    phys_flux<D>(ar, l, n, fl);
+    phys_flux<D>(ar, r, n, fr);
+    const double c1 = ar.mul(lambda_l, lambda_r);
     const double c2 = lambda_r - lambda_l;
-    const double c2inv = 1 / c2;
-    solution_delta<D>(l, r, du);
+    const double c2inv = ar.quo(1, c2);
+    solution_delta<D>(ar, l, r, du);
 #pragma unroll
     for (int i = 0; i < D + 2; ++i)
-      f[i] = c2inv * (lambda_r * fl[i] - lambda_l * fr[i] + c1 * du[i]);
+      f[i] = ar.mul(c2inv, ar.mul(lambda_r, fl[i]) - ar.mul(lambda_l, fr[i]) + ar.mul(c1, du[i]));
   }
 }
 
-template <int D>
-__device__ __forceinline__ void rusanov(const prim<D> &l, const prim<D> &r,
+template <int D, class A>
+__device__ __forceinline__ void rusanov(A &ar, const prim<D> &l, const prim<D> &r,
                                         const double *n, double *f) {
   double fl[D + 2], fr[D + 2], du[D + 2];
-  phys_flux<D>(l, n, fl);
-  phys_flux<D>(r, n, fr);
-  const double sl = l.a + fabs(dot<D>(l.v, n));
-  const double sr = r.a + fabs(dot<D>(r.v, n));
+  phys_flux<D>(ar, l, n, fl);
+  phys_flux<D>(ar, r, n, fr);
+  const double sl = l.a + absval(dot<D>(ar, l.v, n));
+  const double sr = r.a + absval(dot<D>(ar, r.v, n));
   const double s = smax(sl, sr);
-  solution_delta<D>(l, r, du);
-  const double half_s = s / 2;
+  solution_delta<D>(ar, l, r, du);
+  const double half_s = ar.quo(s, 2);
 #pragma unroll
-  for (int i = 0; i < D + 2; ++i) f[i] = (fl[i] + fr[i]) / 2 - du[i] * half_s;
+  for (int i = 0; i < D + 2; ++i) f[i] = ar.quo(fl[i] + fr[i], 2) - ar.mul(du[i], half_s);
 }
 
 // Toro's HLLC (sec. 10.4) with the hlle_flux wave-speed estimates.
-template <int D>
-__device__ __forceinline__ void hllc(const prim<D> &l, const prim<D> &r,
+template <int D, class A>
+__device__ __forceinline__ void hllc(A &ar, const prim<D> &l, const prim<D> &r,
                                      const double *n, double *f) {
-  const double vnl = dot<D>(l.v, n), vnr = dot<D>(r.v, n);
+  const double vnl = dot<D>(ar, l.v, n), vnr = dot<D>(ar, r.v, n);
   const double sL = smin(vnl - l.a, vnr - r.a);
   const double sR = smax(vnl + l.a, vnr + r.a);
-  if (sL >= 0) {
-    phys_flux<D>(l, n, f);
+  if (ge0(sL)) {
+    phys_flux<D>(ar, l, n, f);
     return;
   }
-  if (sR <= 0) {
-    phys_flux<D>(r, n, f);
+  if (le0(sR)) {
+    phys_flux<D>(ar, r, n, f);
     return;
   }
-  const double ml = l.d * (sL - vnl);
-  const double mr = r.d * (sR - vnr);
-  const double sM = (r.p - l.p + ml * vnl - mr * vnr) / (ml - mr);
-  const bool left = sM >= 0;
+  const double ml = ar.mul(l.d, sL - vnl);
+  const double mr = ar.mul(r.d, sR - vnr);
+  const double sM = ar.quo(r.p - l.p + ar.mul(ml, vnl) - ar.mul(mr, vnr), ml - mr);
+  const bool left = ge0(sM);
   const prim<D> &u = left ? l : r;
   const double sK = left ? sL : sR;
   const double mK = left ? ml : mr;
   const double vnK = left ? vnl : vnr;
   double fk[D + 2];
-  phys_flux<D>(u, n, fk);
-  const double EK = u.d * total_energy<D>(u);
-  const double fac = mK / (sK - sM);
+  phys_flux<D>(ar, u, n, fk);
+  const double EK = ar.mul(u.d, total_energy<D>(ar, u));
+  const double fac = ar.quo(mK, sK - sM);
   const double dvn = sM - vnK;
-  f[0] = fk[0] + sK * (fac - u.d);
+  f[0] = fk[0] + ar.mul(sK, fac - u.d);
 #pragma unroll
   for (int i = 0; i < D; ++i)
-    f[1 + i] = fk[1 + i] + sK * (fac * (u.v[i] + dvn * n[i]) - u.d * u.v[i]);
-  f[D + 1] = fk[D + 1] + sK * (fac * (EK / u.d + dvn * (sM + u.p / mK)) - EK);
+    f[1 + i] = fk[1 + i] +
+               ar.mul(sK, ar.mul(fac, u.v[i] + ar.mul(dvn, n[i])) - ar.mul(u.d, u.v[i]));
+  f[D + 1] = fk[D + 1] +
+             ar.mul(sK, ar.mul(fac, ar.quo(EK, u.d) + ar.mul(dvn, sM + ar.quo(u.p, mK))) - EK);
 }
 
 // ---------------------------------------------------------------------------
-// Order-preserving integer keys of doubles.  Comparisons, minima and maxima of
-// doubles run on the integer pipe through these keys (the FP64 pipe of this
-// chip is narrow).  key(a) < key(b) exactly when a < b for non-NaN values;
-// -0 and +0 share the key of +0, so a minimum or maximum can differ from the
-// floating-point one only in the sign of a zero.
+// Order-preserving integer keys of doubles.  Minima and maxima of doubles run
+// on the integer pipe through these keys.  key(a) < key(b) exactly when a < b
+// for non-NaN values; -0 and +0 share the key of +0, so a minimum or maximum
+// can differ from the floating-point one only in the sign of a zero.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ long long okey(double x) {
   long long b = __double_as_longlong(x);
@@ -167,6 +247,30 @@ __device__ __forceinline__ double from_okey(long long k) {
 // With PRE the V/A of each (cell, face) slot comes from a table built once per
 // mesh by the same division.
 // ---------------------------------------------------------------------------
+template <int D, bool PRE, class A>
+__device__ __forceinline__ double cell_dt_inv(A &ar, const fvh_mesh_view &m,
+                                              const fvh_state_view &s, int c,
+                                              const double *__restrict__ slot_dx) {
+  double v[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) v[i] = s.velocity[i][c];
+  const double a = s.sound_speed[c];
+  const double vol = PRE ? 0.0 : m.cell_volume[c];
+  double dt_inv = 0;
+  const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
+  for (int q = q0; q < q1; ++q) {
+    int f = m.cell_faces[q];
+    f = f < 0 ? ~f : f;
+    double n[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) n[i] = m.face_normal[i][f];
+    const double delta_x = PRE ? slot_dx[q] : ar.quo(vol, m.face_area[f]);
+    const double dti = ar.quo(a + absval(dot<D>(ar, v, n)), delta_x);
+    dt_inv = smax(dti, dt_inv);
+  }
+  return dt_inv;
+}
+
 template <int D, bool PRE>
 __global__ void __launch_bounds__(kDtThreads)
 dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial,
@@ -174,22 +278,15 @@ dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial
   double dt_inv = 0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.num_cells;
        c += gridDim.x * blockDim.x) {
-    double v[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i) v[i] = s.velocity[i][c];
-    const double a = s.sound_speed[c];
-    const double vol = PRE ? 0.0 : m.cell_volume[c];
-    const int q0 = m.cell_face_offsets[c], q1 = m.cell_face_offsets[c + 1];
-    for (int q = q0; q < q1; ++q) {
-      int f = m.cell_faces[q];
-      f = f < 0 ? ~f : f;
-      double n[D];
-#pragma unroll
-      for (int i = 0; i < D; ++i) n[i] = m.face_normal[i][f];
-      const double delta_x = PRE ? slot_dx[q] : vol / m.face_area[f];
-      const double dti = (a + fabs(dot<D>(v, n))) / delta_x;
-      dt_inv = smax(dti, dt_inv);
+    arith_opt ar;
+    double cell = cell_dt_inv<D, PRE>(ar, m, s, c, slot_dx);
+    if (ar.rare) {
+      arith_hw hw;
+      cell = cell_dt_inv<D, PRE>(hw, m, s, c, slot_dx);
     }
+    // the reference's running maximum over cells and faces, taken cell by
+    // cell (a maximum of maxima: the same value)
+    dt_inv = smax(cell, dt_inv);
   }
   dt_inv = block_max(dt_inv);
   if (threadIdx.x == 0) partial[blockIdx.x] = dt_inv;
@@ -203,12 +300,12 @@ dt_final_kernel(const double *partial, int nblocks, fvh_params p,
   dt_inv = block_max(dt_inv);
   if (threadIdx.x == 0) {
     const double max_dt = p.final_time - soln_time[0];
-    if (dt_inv <= 0) {
+    if (le0(dt_inv)) {
       atomicMin(status, status_key(0, FVH_ERR_INFINITE_DT));
       dt_out[0] = 0;
     } else {
-      double time_step = 1 / dt_inv;
-      time_step *= p.cfl;
+      double time_step = __ddiv_rn(1, dt_inv);
+      time_step = __dmul_rn(time_step, p.cfl);
       dt_out[0] = smin(time_step, max_dt);
     }
   }
@@ -218,18 +315,6 @@ dt_final_kernel(const double *partial, int nblocks, fvh_params p,
 // Geometry-only tables built once per mesh for the solver (same operations in
 // the same order as the on-the-fly code, so the values are identical).
 // ---------------------------------------------------------------------------
-template <int D>
-__global__ void slot_dx_kernel(const fvh_mesh_view m, double *slot_dx) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.num_cells) return;
-  const double vol = m.cell_volume[c];
-  for (int q = m.cell_face_offsets[c]; q < m.cell_face_offsets[c + 1]; ++q) {
-    int f = m.cell_faces[q];
-    f = f < 0 ? ~f : f;
-    slot_dx[q] = vol / m.face_area[f];
-  }
-}
-
 // lsq record per cell: 2D (a00 a01 a11 denom); 3D (a00 a01 a02 a11 a12 a22
 // min1 min2 min3 denom), tasks.h:210-228 and :250-261
 template <int D>
@@ -237,8 +322,8 @@ struct lsq_width {
   static constexpr int value = D == 2 ? 4 : 10;
 };
 
-template <int D>
-__device__ __forceinline__ void lsq_matrix(const fvh_mesh_view &m, int c0, double *r) {
+template <int D, class A>
+__device__ __forceinline__ void lsq_matrix(A &ar, const fvh_mesh_view &m, int c0, double *r) {
   double x0[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
@@ -249,77 +334,128 @@ __device__ __forceinline__ void lsq_matrix(const fvh_mesh_view &m, int c0, doubl
 #pragma unroll
     for (int d = 0; d < D; ++d) dx[d] = m.cell_centroid[d][c1] - x0[d];
     if (D == 2) {
-      dxdx[0] += dx[0] * dx[0];
-      dxdx[1] += dx[0] * dx[1];
-      dxdx[2] += dx[1] * dx[1];
+      dxdx[0] += ar.mul(dx[0], dx[0]);
+      dxdx[1] += ar.mul(dx[0], dx[1]);
+      dxdx[2] += ar.mul(dx[1], dx[1]);
     } else {
-      dxdx[0] += dx[0] * dx[0];
-      dxdx[1] += dx[0] * dx[1];
-      dxdx[2] += dx[0] * dx[D - 1];
-      dxdx[3] += dx[1] * dx[1];
-      dxdx[4] += dx[1] * dx[D - 1];
-      dxdx[5] += dx[D - 1] * dx[D - 1];
+      dxdx[0] += ar.mul(dx[0], dx[0]);
+      dxdx[1] += ar.mul(dx[0], dx[1]);
+      dxdx[2] += ar.mul(dx[0], dx[D - 1]);
+      dxdx[3] += ar.mul(dx[1], dx[1]);
+      dxdx[4] += ar.mul(dx[1], dx[D - 1]);
+      dxdx[5] += ar.mul(dx[D - 1], dx[D - 1]);
     }
   }
   if (D == 2) {
     r[0] = dxdx[0];
     r[1] = dxdx[1];
     r[2] = dxdx[2];
-    r[3] = 1 / (dxdx[0] * dxdx[2] - dxdx[1] * dxdx[1]);
+    r[3] = ar.quo(1, ar.mul(dxdx[0], dxdx[2]) - ar.mul(dxdx[1], dxdx[1]));
   } else {
     const double a00 = dxdx[0], a01 = dxdx[1], a02 = dxdx[2], a11 = dxdx[3],
                  a12 = dxdx[4], a22 = dxdx[5];
-    const double min1 = a11 * a22 - a12 * a12;
-    const double min2 = a01 * a22 - a12 * a02;
-    const double min3 = a01 * a12 - a11 * a02;
+    const double min1 = ar.mul(a11, a22) - ar.mul(a12, a12);
+    const double min2 = ar.mul(a01, a22) - ar.mul(a12, a02);
+    const double min3 = ar.mul(a01, a12) - ar.mul(a11, a02);
     for (int k = 0; k < 6; ++k) r[k] = dxdx[k];
     r[6] = min1;
     r[7] = min2;
     r[8] = min3;
-    r[9] = 1 / (a00 * min1 - a01 * min2 + a02 * min3);
+    r[9] = ar.quo(1, ar.mul(a00, min1) - ar.mul(a01, min2) + ar.mul(a02, min3));
   }
 }
 
 template <int D>
-__global__ void lsq_kernel(const fvh_mesh_view m, double *lsq) {
+__global__ void cell_tables_kernel(const fvh_mesh_view m, double *lsq, double *slot_dx,
+                                   double *nbr_dx, double *vtx_dx) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.num_cells) return;
+  arith_hw hw;  // set-up, once per mesh
   constexpr int W = lsq_width<D>::value;
   double r[W];
-  lsq_matrix<D>(m, c, r);
+  lsq_matrix<D>(hw, m, c, r);
 #pragma unroll
   for (int k = 0; k < W; ++k) lsq[(size_t)k * m.num_cells + c] = r[k];
+  const double vol = m.cell_volume[c];
+  for (int q = m.cell_face_offsets[c]; q < m.cell_face_offsets[c + 1]; ++q) {
+    int f = m.cell_faces[q];
+    f = f < 0 ? ~f : f;
+    slot_dx[q] = hw.quo(vol, m.face_area[f]);
+  }
+  double x0[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c];
+  for (int q = m.cell_nbr_offsets[c]; q < m.cell_nbr_offsets[c + 1]; ++q) {
+    const int c1 = m.cell_nbrs[q];
+#pragma unroll
+    for (int d = 0; d < D; ++d) nbr_dx[(size_t)q * D + d] = m.cell_centroid[d][c1] - x0[d];
+  }
+  for (int q = m.cell_vertex_offsets[c]; q < m.cell_vertex_offsets[c + 1]; ++q) {
+    const int v = m.cell_vertices[q];
+#pragma unroll
+    for (int d = 0; d < D; ++d) vtx_dx[(size_t)q * D + d] = m.vertex_coord[d][v] - x0[d];
+  }
+}
+
+template <int D>
+__global__ void face_tables_kernel(const fvh_mesh_view m, double *face_dx) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.num_faces) return;
+  const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int c = side == 0 ? cc.x : cc.y;
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+      face_dx[(size_t)f * 2 * D + side * D + i] =
+          c >= 0 ? m.face_centroid[i][f] - m.cell_centroid[i][c] : 0.0;
+  }
 }
 
 // ---------------------------------------------------------------------------
 // gradients + Barth-Jespersen vertex limiter (tasks.h:145-321)
-// With PRE the geometry-only matrix terms come from the lsq table.
+// With PRE the geometry-only terms (matrix, neighbour and vertex offsets) come
+// from the solver's tables.
 // ---------------------------------------------------------------------------
-template <int D, bool LIMIT, bool PRE>
-__global__ void __launch_bounds__(kCellThreads)
-gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
-                 const double *__restrict__ lsq) {
+template <int D>
+__device__ __forceinline__ void load_dx(const double *__restrict__ p, double *dx) {
+  if (D == 2) {
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    dx[0] = v.x;
+    dx[D - 1] = v.y;
+  } else {
+#pragma unroll
+    for (int d = 0; d < D; ++d) dx[d] = __ldg(p + d);
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void load_values(const fvh_state_view &s, int c, double *u) {
+  int i = 0;
+  u[i++] = s.density[c];
+#pragma unroll
+  for (int d = 0; d < D; ++d) u[i++] = s.velocity[d][c];
+  u[i++] = s.internal_energy[c];
+  u[i++] = s.pressure[c];
+  u[i++] = s.sound_speed[c];
+}
+
+// The limited gradients gu of cell c0 (rows: the reconstructed variables d,
+// v.., e, p, a).
+template <int D, bool LIMIT, bool PRE, class A>
+__device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
+                                               const fvh_state_view &s, const tables &t,
+                                               int c0, double (&gu)[D + 4][D]) {
   constexpr int NV = D + 4;
   constexpr int W = lsq_width<D>::value;
   constexpr double tol = 1.e-9;
-  const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c0 >= m.num_cells) return;
   double x0[D];
+  if (!PRE) {
 #pragma unroll
-  for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
-  double u0[NV];
-  long long kmin[NV], kmax[NV];  // umin / umax as order keys
-  {
-    int i = 0;
-    u0[i++] = s.density[c0];
-#pragma unroll
-    for (int d = 0; d < D; ++d) u0[i++] = s.velocity[d][c0];
-    u0[i++] = s.internal_energy[c0];
-    u0[i++] = s.pressure[c0];
-    u0[i++] = s.sound_speed[c0];
+    for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
   }
-#pragma unroll
-  for (int k = 0; k < NV; ++k) kmin[k] = kmax[k] = okey(u0[k]);
+  double u0[NV];
+  load_values<D>(s, c0, u0);
   double dudx[NV][D];
 #pragma unroll
   for (int k = 0; k < NV; ++k)
@@ -329,42 +465,44 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
   for (int q = q0; q < q1; ++q) {
     const int c1 = m.cell_nbrs[q];
     double u1[NV];
-    {
-      int i = 0;
-      u1[i++] = s.density[c1];
-#pragma unroll
-      for (int d = 0; d < D; ++d) u1[i++] = s.velocity[d][c1];
-      u1[i++] = s.internal_energy[c1];
-      u1[i++] = s.pressure[c1];
-      u1[i++] = s.sound_speed[c1];
-    }
+    load_values<D>(s, c1, u1);
     double dx[D];
+    if (PRE) {
+      load_dx<D>(t.nbr_dx + (size_t)q * D, dx);
+    } else {
 #pragma unroll
-    for (int d = 0; d < D; ++d) dx[d] = m.cell_centroid[d][c1] - x0[d];
+      for (int d = 0; d < D; ++d) dx[d] = m.cell_centroid[d][c1] - x0[d];
+    }
+    double du[NV];
+    unsigned nonzero = 0;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      const long long k1 = okey(u1[k]);
-      kmin[k] = (k1 < kmin[k]) ? k1 : kmin[k];  // std::min(u1, umin)
-      kmax[k] = (kmax[k] < k1) ? k1 : kmax[k];  // std::max(u1, umax)
-      const double du = u1[k] - u0[k];
+      du[k] = u1[k] - u0[k];
+      nonzero |= (unsigned)!is_zero(du[k]);
+    }
+    // a neighbour equal to the cell in every variable adds (+-0) * dx = +-0 to
+    // each sum, which leaves it as it is (a sum that starts at +0 and adds
+    // nonzero terms is never -0): cells inside a uniform region skip it
+    if (nonzero) {
 #pragma unroll
-      for (int j = 0; j < D; ++j) dudx[k][j] += du * dx[j];
+      for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int j = 0; j < D; ++j) dudx[k][j] += ar.mul(du[k], dx[j]);
     }
   }
   double r[W];
   if (PRE) {
 #pragma unroll
-    for (int k = 0; k < W; ++k) r[k] = lsq[(size_t)k * m.num_cells + c0];
+    for (int k = 0; k < W; ++k) r[k] = t.lsq[(size_t)k * m.num_cells + c0];
   } else {
-    lsq_matrix<D>(m, c0, r);
+    lsq_matrix<D>(ar, m, c0, r);
   }
-  double gu[NV][D];
   if (D == 2) {
     const double a00 = r[0], a01 = r[1], a11 = r[2], denom = r[3];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      gu[k][0] = (dudx[k][0] * a11 - dudx[k][1] * a01) * denom;
-      gu[k][1] = (dudx[k][1] * a00 - dudx[k][0] * a01) * denom;
+      gu[k][0] = ar.mul(ar.mul(dudx[k][0], a11) - ar.mul(dudx[k][1], a01), denom);
+      gu[k][D - 1] = ar.mul(ar.mul(dudx[k][1], a00) - ar.mul(dudx[k][0], a01), denom);
     }
   } else {
     const double a00 = r[0], a01 = r[1], a02 = r[2], a11 = r[3], a12 = r[4], a22 = r[5];
@@ -372,9 +510,16 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       const double b0 = dudx[k][0], b1 = dudx[k][1], b2 = dudx[k][D - 1];
-      gu[k][0] = (b0 * min1 - a01 * (b1 * a22 - a12 * b2) + a02 * (b1 * a12 - a11 * b2)) * denom;
-      gu[k][1] = (a00 * (b1 * a22 - a12 * b2) - b0 * min2 + a02 * (b2 * a01 - a02 * b1)) * denom;
-      gu[k][D - 1] = (a00 * (b2 * a11 - a12 * b1) - a01 * (b2 * a01 - a02 * b1) + b0 * min3) * denom;
+      gu[k][0] = ar.mul(ar.mul(b0, min1) - ar.mul(a01, ar.mul(b1, a22) - ar.mul(a12, b2)) +
+                            ar.mul(a02, ar.mul(b1, a12) - ar.mul(a11, b2)),
+                        denom);
+      gu[k][1] = ar.mul(ar.mul(a00, ar.mul(b1, a22) - ar.mul(a12, b2)) - ar.mul(b0, min2) +
+                            ar.mul(a02, ar.mul(b2, a01) - ar.mul(a02, b1)),
+                        denom);
+      gu[k][D - 1] = ar.mul(ar.mul(a00, ar.mul(b2, a11) - ar.mul(a12, b1)) -
+                                ar.mul(a01, ar.mul(b2, a01) - ar.mul(a02, b1)) +
+                                ar.mul(b0, min3),
+                            denom);
     }
   }
   if (LIMIT) {
@@ -384,41 +529,102 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
     // result equals the reference's per-vertex minimum.
     const long long ktol = okey(tol), kntol = okey(-tol);
     long long kpos[NV], kneg[NV];
+    // a variable with a zero gradient has u1 == u0 at every vertex (to the
+    // sign of a zero, which the order keys do not see): no vertex limits it
+    bool graded[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) kpos[k] = kneg[k] = 0;
+    for (int k = 0; k < NV; ++k) {
+      kpos[k] = kneg[k] = 0;
+      graded[k] = false;
+#pragma unroll
+      for (int i = 0; i < D; ++i) graded[k] = graded[k] || !is_zero(gu[k][i]);
+    }
     const int r0 = m.cell_vertex_offsets[c0], r1 = m.cell_vertex_offsets[c0 + 1];
     for (int rr = r0; rr < r1; ++rr) {
-      const int vtx = m.cell_vertices[rr];
       double dxv[D];
+      if (PRE) {
+        load_dx<D>(t.vtx_dx + (size_t)rr * D, dxv);
+      } else {
+        const int vtx = m.cell_vertices[rr];
 #pragma unroll
-      for (int i = 0; i < D; ++i) dxv[i] = m.vertex_coord[i][vtx] - x0[i];
+        for (int i = 0; i < D; ++i) dxv[i] = m.vertex_coord[i][vtx] - x0[i];
+      }
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
+        if (!graded[k]) continue;
         double u1 = u0[k];
 #pragma unroll
-        for (int i = 0; i < D; ++i) u1 += dxv[i] * gu[k][i];
+        for (int i = 0; i < D; ++i) u1 += ar.mul(dxv[i], gu[k][i]);
         const long long kd = okey(u1 - u0[k]);
         if (kd > ktol) kpos[k] = (kpos[k] < kd) ? kd : kpos[k];
         else if (kd < kntol) kneg[k] = (kd < kneg[k]) ? kd : kneg[k];
       }
     }
+    // the neighbour extrema umin / umax (tasks.h:232-236) are needed only for
+    // a variable some vertex value departs from by more than tol: they are
+    // taken then, in a second pass over the neighbours (whose values are
+    // still in cache), as order keys
+    const double *plane[NV];
+    {
+      int i = 0;
+      plane[i++] = s.density;
+#pragma unroll
+      for (int d = 0; d < D; ++d) plane[i++] = s.velocity[d];
+      plane[i++] = s.internal_energy;
+      plane[i++] = s.pressure;
+      plane[i++] = s.sound_speed;
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       long long kphi = okey(1.0);
-      if (kpos[k] > ktol) {
-        const long long kq = okey((from_okey(kmax[k]) - u0[k]) / from_okey(kpos[k]));
-        kphi = (kq < kphi) ? kq : kphi;
-      }
-      if (kneg[k] < kntol) {
-        const long long kq = okey((from_okey(kmin[k]) - u0[k]) / from_okey(kneg[k]));
-        kphi = (kq < kphi) ? kq : kphi;
+      if (kpos[k] > ktol || kneg[k] < kntol) {
+        long long kmin = okey(u0[k]), kmax = kmin;
+        for (int q = q0; q < q1; ++q) {
+          const long long k1 = okey(plane[k][m.cell_nbrs[q]]);
+          kmin = (k1 < kmin) ? k1 : kmin;  // std::min(u1, umin)
+          kmax = (kmax < k1) ? k1 : kmax;  // std::max(u1, umax)
+        }
+        // RN(N / du) >= 1 exactly when |N| >= |du| (N and du of one sign, du
+        // normal), so the quotient is formed only when it can lower phi below 1
+        if (kpos[k] > ktol) {
+          const double num = from_okey(kmax) - u0[k];
+          if (okey(num) < kpos[k]) {
+            const long long kq = okey(ar.quo(num, from_okey(kpos[k])));
+            kphi = (kq < kphi) ? kq : kphi;
+          }
+        }
+        if (kneg[k] < kntol) {
+          const double num = from_okey(kmin) - u0[k];
+          if (okey(num) > kneg[k]) {
+            const long long kq = okey(ar.quo(num, from_okey(kneg[k])));
+            kphi = (kq < kphi) ? kq : kphi;
+          }
+        }
       }
       kphi = (kphi < 0) ? 0 : kphi;  // std::max(phi, 0)
       if (kphi != okey(1.0)) {
         const double phi = from_okey(kphi);
 #pragma unroll
-        for (int i = 0; i < D; ++i) gu[k][i] *= phi;
+        for (int i = 0; i < D; ++i) gu[k][i] = ar.mul(gu[k][i], phi);
       }
+    }
+  }
+}
+
+template <int D, bool LIMIT, bool PRE>
+__global__ void __launch_bounds__(kCellThreads)
+gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
+                 const tables t) {
+  constexpr int NV = D + 4;
+  const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c0 >= m.num_cells) return;
+  double gu[NV][D];
+  {
+    arith_opt ar;
+    cell_gradients<D, LIMIT, PRE>(ar, m, s, t, c0, gu);
+    if (ar.rare) {
+      arith_hw hw;
+      cell_gradients<D, LIMIT, PRE>(hw, m, s, t, c0, gu);
     }
   }
 #pragma unroll
@@ -436,11 +642,10 @@ gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradie
 // ---------------------------------------------------------------------------
 // face fluxes (tasks.h:385-464)
 // ---------------------------------------------------------------------------
-template <int D, bool SECOND>
-__device__ __forceinline__ prim<D> reconstruct(const fvh_mesh_view &m,
-                                               const fvh_state_view &s,
+template <int D, bool SECOND, class A>
+__device__ __forceinline__ prim<D> reconstruct(A &ar, const fvh_state_view &s,
                                                const fvh_gradient_view &g, int c,
-                                               const double *fx, bool swap) {
+                                               const double *dx, bool swap) {
   prim<D> w;
   w.d = s.density[c];
 #pragma unroll
@@ -449,75 +654,122 @@ __device__ __forceinline__ prim<D> reconstruct(const fvh_mesh_view &m,
   w.e = s.internal_energy[c];
   w.a = s.sound_speed[c];
   if (SECOND) {
-    double dx[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i) dx[i] = fx[i] - m.cell_centroid[i][c];
     double *const *gp = swap ? g.internal_energy : g.pressure;
     double *const *ge = swap ? g.pressure : g.internal_energy;
+    double gd[D], gv[D][D], gpp[D], gee[D], ga[D];
+    unsigned nonzero = 0;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      w.d += dx[i] * g.density[i][c];
+      gd[i] = g.density[i][c];
+      nonzero |= (unsigned)!is_zero(gd[i]);
 #pragma unroll
-      for (int d = 0; d < D; ++d) w.v[d] += dx[i] * g.velocity[d][i][c];
-      w.p += dx[i] * gp[i][c];
-      w.e += dx[i] * ge[i][c];
-      w.a += dx[i] * g.sound_speed[i][c];
+      for (int d = 0; d < D; ++d) {
+        gv[d][i] = g.velocity[d][i][c];
+        nonzero |= (unsigned)!is_zero(gv[d][i]);
+      }
+      gpp[i] = gp[i][c];
+      gee[i] = ge[i][c];
+      ga[i] = g.sound_speed[i][c];
+      nonzero |= (unsigned)(!is_zero(gpp[i]) | !is_zero(gee[i]) | !is_zero(ga[i]));
+    }
+    // zero gradients add dx * (+-0) = +-0 to each value (dx is finite), which
+    // leaves it as it is unless the value is -0 or a NaN: cells with uniform
+    // neighbourhoods skip the products when no value is one of those
+    unsigned plain = (unsigned)(ordinary(w.d) & ordinary(w.p) & ordinary(w.e) & ordinary(w.a));
+#pragma unroll
+    for (int d = 0; d < D; ++d) plain &= (unsigned)ordinary(w.v[d]);
+    if (nonzero | !plain) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        w.d += ar.mul(dx[i], gd[i]);
+#pragma unroll
+        for (int d = 0; d < D; ++d) w.v[d] += ar.mul(dx[i], gv[d][i]);
+        w.p += ar.mul(dx[i], gpp[i]);
+        w.e += ar.mul(dx[i], gee[i]);
+        w.a += ar.mul(dx[i], ga[i]);
+      }
     }
   }
   return w;
 }
 
-template <int D, int KIND, bool SECOND>
-__global__ void __launch_bounds__(kFaceThreads)
-fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
-              const fvh_flux_view fl, int swap, int outflow) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= m.num_faces) return;
-  const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
-  double n[D], fx[D];
+// x_f - x_c of one side of face f, from the table or on the fly
+template <int D, bool PRE>
+__device__ __forceinline__ void face_offset(const fvh_mesh_view &m, const double *face_dx,
+                                            int f, int side, int c, double *dx) {
+  if (PRE) {
+    load_dx<D>(face_dx + (size_t)f * 2 * D + side * D, dx);
+  } else {
 #pragma unroll
-  for (int i = 0; i < D; ++i) {
-    n[i] = m.face_normal[i][f];
-    fx[i] = m.face_centroid[i][f];
+    for (int i = 0; i < D; ++i) dx[i] = m.face_centroid[i][f] - m.cell_centroid[i][c];
   }
-  const prim<D> wl = reconstruct<D, SECOND>(m, s, g, cc.x, fx, swap != 0);
-  double F[D + 2];
+}
+
+// the area-weighted flux of face f (tasks.h:405-461)
+template <int D, int KIND, bool SECOND, bool PRE, class A>
+__device__ __forceinline__ void face_flux(A &ar, const fvh_mesh_view &m,
+                                          const fvh_state_view &s, const fvh_gradient_view &g,
+                                          int f, int2 cc, bool swap, bool outflow,
+                                          const double *face_dx, double *F) {
+  double n[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) n[i] = m.face_normal[i][f];
+  double dx[D] = {};
+  if (SECOND) face_offset<D, PRE>(m, face_dx, f, 0, cc.x, dx);
+  const prim<D> wl = reconstruct<D, SECOND>(ar, s, g, cc.x, dx, swap);
   if (cc.y >= 0) {
-    const prim<D> wr = reconstruct<D, SECOND>(m, s, g, cc.y, fx, swap != 0);
+    if (SECOND) face_offset<D, PRE>(m, face_dx, f, 1, cc.y, dx);
+    const prim<D> wr = reconstruct<D, SECOND>(ar, s, g, cc.y, dx, swap);
     if (KIND == FVH_FLUX_RUSANOV)
-      rusanov<D>(wl, wr, n, F);
+      rusanov<D>(ar, wl, wr, n, F);
     else if (KIND == FVH_FLUX_HLLC)
-      hllc<D>(wl, wr, n, F);
+      hllc<D>(ar, wl, wr, n, F);
     else
-      hlle<D>(wl, wr, n, F);
+      hlle<D>(ar, wl, wr, n, F);
   } else if (outflow) {
-    phys_flux<D>(wl, n, F);
+    phys_flux<D>(ar, wl, n, F);
   } else {
     F[0] = 0;
 #pragma unroll
-    for (int i = 0; i < D; ++i) F[1 + i] = wl.p * n[i];
+    for (int i = 0; i < D; ++i) F[1 + i] = ar.mul(wl.p, n[i]);
     F[D + 1] = 0;
   }
   const double area = m.face_area[f];
-  fl.mass[f] = F[0] * area;
 #pragma unroll
-  for (int i = 0; i < D; ++i) fl.momentum[i][f] = F[1 + i] * area;
-  fl.energy[f] = F[D + 1] * area;
+  for (int k = 0; k < D + 2; ++k) F[k] = ar.mul(F[k], area);
+}
+
+template <int D, int KIND, bool SECOND, bool PRE>
+__global__ void __launch_bounds__(kFaceThreads)
+fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
+              const fvh_flux_view fl, int swap, int outflow, const double *__restrict__ face_dx) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.num_faces) return;
+  const int2 cc = reinterpret_cast<const int2 *>(m.face_cells)[f];
+  double F[D + 2];
+  {
+    arith_opt ar;
+    face_flux<D, KIND, SECOND, PRE>(ar, m, s, g, f, cc, swap != 0, outflow != 0, face_dx, F);
+    if (ar.rare) {
+      arith_hw hw;
+      face_flux<D, KIND, SECOND, PRE>(hw, m, s, g, f, cc, swap != 0, outflow != 0, face_dx, F);
+    }
+  }
+  fl.mass[f] = F[0];
+#pragma unroll
+  for (int i = 0; i < D; ++i) fl.momentum[i][f] = F[1 + i];
+  fl.energy[f] = F[D + 1];
 }
 
 // ---------------------------------------------------------------------------
 // gather + conservative update + EOS (tasks.h:589-659)
 // ---------------------------------------------------------------------------
-template <int D>
-__global__ void __launch_bounds__(kCellThreads)
-update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_view s,
-              const double *dt, double factor, double gamma, double cv,
-              double *soln_time, fvh_device_status *status) {
-  double delta_t = dt[0];
-  delta_t *= factor;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c == 0) soln_time[0] = 0.0 + soln_time[0] + delta_t;
-  if (c >= m.num_cells) return;
+// the new state of cell c: w = (d, v.., e, p, T, a^2)
+template <int D, class A>
+__device__ __forceinline__ void cell_update(A &ar, const fvh_mesh_view &m,
+                                            const fvh_flux_view &fl, const fvh_state_view &s,
+                                            int c, double delta_t, double gamma, double cv,
+                                            double *w) {
   double du[D + 2];
 #pragma unroll
   for (int k = 0; k < D + 2; ++k) du[k] = 0;
@@ -538,27 +790,95 @@ update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_vie
       for (int k = 0; k < D + 2; ++k) du[k] += F[k];
     }
   }
-  const double scale = delta_t / m.cell_volume[c];
+  const double scale = ar.quo(delta_t, m.cell_volume[c]);
 #pragma unroll
-  for (int k = 0; k < D + 2; ++k) du[k] *= scale;
+  for (int k = 0; k < D + 2; ++k) du[k] = ar.mul(du[k], scale);
   double vel[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) vel[i] = s.velocity[i][c];
   const double den0 = s.density[c];
   const double mass = den0 + du[0];
-  const double ener = den0 * (s.internal_energy[c] + 0.5 * dot<D>(vel, vel)) + du[D + 1];
-  const double inv_mass = 1 / mass;
+  const double ener =
+      ar.mul(den0, s.internal_energy[c] + ar.mul(0.5, dot<D>(ar, vel, vel))) + du[D + 1];
+  const double inv_mass = ar.quo(1, mass);
 #pragma unroll
-  for (int i = 0; i < D; ++i) vel[i] = (den0 * vel[i] + du[1 + i]) * inv_mass;
-  const double e = ener * inv_mass - 0.5 * dot<D>(vel, vel);
-  s.density[c] = mass;
+  for (int i = 0; i < D; ++i) vel[i] = ar.mul(ar.mul(den0, vel[i]) + du[1 + i], inv_mass);
+  const double e = ar.mul(ener, inv_mass) - ar.mul(0.5, dot<D>(ar, vel, vel));
+  w[0] = mass;
 #pragma unroll
-  for (int i = 0; i < D; ++i) s.velocity[i][c] = vel[i];
-  s.internal_energy[c] = e;
-  s.pressure[c] = (gamma - 1.0) * mass * e;
-  s.temperature[c] = cv == 1.0 ? e : e / cv;  // x / 1 == x exactly
-  s.sound_speed[c] = sqrt(gamma * (gamma - 1.0) * e);
-  if (e < 0 || mass < 0) atomicMin(status, status_key(c, FVH_ERR_NEGATIVE_STATE));
+  for (int i = 0; i < D; ++i) w[1 + i] = vel[i];
+  w[D + 1] = e;
+  w[D + 2] = ar.mul(ar.mul(gamma - 1.0, mass), e);
+  w[D + 3] = cv == 1.0 ? e : ar.quo(e, cv);          // x / 1 == x exactly
+  w[D + 4] = ar.mul(ar.mul(gamma, gamma - 1.0), e);  // a^2; its root is taken once
+}
+
+template <int D>
+__global__ void __launch_bounds__(kCellThreads)
+update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_view s,
+              const double *dt, double factor, double gamma, double cv,
+              double *soln_time, fvh_device_status *status) {
+  const double delta_t = __dmul_rn(dt[0], factor);
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c == 0) soln_time[0] = 0.0 + soln_time[0] + delta_t;
+  if (c >= m.num_cells) return;
+  double w[D + 5];
+  {
+    arith_opt ar;
+    cell_update<D>(ar, m, fl, s, c, delta_t, gamma, cv, w);
+    if (ar.rare) {
+      arith_hw hw;
+      cell_update<D>(hw, m, fl, s, c, delta_t, gamma, cv, w);
+    }
+  }
+  s.density[c] = w[0];
+#pragma unroll
+  for (int i = 0; i < D; ++i) s.velocity[i][c] = w[1 + i];
+  s.internal_energy[c] = w[D + 1];
+  s.pressure[c] = w[D + 2];
+  s.temperature[c] = w[D + 3];
+  s.sound_speed[c] = sqrt(w[D + 4]);
+  if (lt0(w[D + 1]) || lt0(w[0])) atomicMin(status, status_key(c, FVH_ERR_NEGATIVE_STATE));
+}
+
+// ---------------------------------------------------------------------------
+// the integer-pipe arithmetic against the FP64 instructions (diagnostic)
+// ---------------------------------------------------------------------------
+__global__ void sf64_kernel(int op, const double *a, const double *b, int64_t n, double *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = a[i], y = b[i];
+    double r;
+    unsigned rare = 0;
+    switch (op) {
+      case 0: r = sf64::mul(x, y); break;
+      case 1: r = sf64::add(x, y); break;
+      case 2: r = sf64::sub(x, y); break;
+      case 3: r = sf64::div(x, y); break;
+      case 4: r = __dmul_rn(x, y); break;
+      case 5: r = __dadd_rn(x, y); break;
+      case 6: r = __dsub_rn(x, y); break;
+      case 7: r = __ddiv_rn(x, y); break;
+      case 8:  // the optimistic forms with their redo, as the kernels use them
+        r = sf64::mul_opt(x, y, rare);
+        if (rare) r = __dmul_rn(x, y);
+        break;
+      default:
+        r = sf64::div_opt(x, y, rare);
+        if (rare) r = __ddiv_rn(x, y);
+        break;
+    }
+    out[i] = r;
+  }
+}
+
+cudaError_t debug_sf64(int op, const double *a, const double *b, int64_t n, double *out,
+                       cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t nb64 = (n + 255) / 256;
+  const int nb = (int)(nb64 < 4096 ? nb64 : 4096);
+  sf64_kernel<<<nb, 256, 0, st>>>(op, a, b, n, out);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -580,54 +900,78 @@ cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
 template <int D>
 cudaError_t launch_gradients(const fvh_mesh_view &m, const fvh_state_view &s,
                              const fvh_gradient_view &g, const fvh_params &p,
-                             cudaStream_t st, const double *lsq) {
+                             cudaStream_t st, const tables &t) {
   const int nb = (m.num_cells + kCellThreads - 1) / kCellThreads;
   const bool lim = p.limiter != FVH_LIMITER_NONE;
-  if (lsq) {
+  if (t.lsq && t.nbr_dx && t.vtx_dx) {
     if (lim)
-      gradients_kernel<D, true, true><<<nb, kCellThreads, 0, st>>>(m, s, g, lsq);
+      gradients_kernel<D, true, true><<<nb, kCellThreads, 0, st>>>(m, s, g, t);
     else
-      gradients_kernel<D, false, true><<<nb, kCellThreads, 0, st>>>(m, s, g, lsq);
+      gradients_kernel<D, false, true><<<nb, kCellThreads, 0, st>>>(m, s, g, t);
   } else {
     if (lim)
-      gradients_kernel<D, true, false><<<nb, kCellThreads, 0, st>>>(m, s, g, nullptr);
+      gradients_kernel<D, true, false><<<nb, kCellThreads, 0, st>>>(m, s, g, t);
     else
-      gradients_kernel<D, false, false><<<nb, kCellThreads, 0, st>>>(m, s, g, nullptr);
+      gradients_kernel<D, false, false><<<nb, kCellThreads, 0, st>>>(m, s, g, t);
   }
   return cudaGetLastError();
 }
 
+size_t table_doubles(int dim, int64_t nc, int64_t nf, int64_t nnz_cf, int64_t nnz_nb,
+                     int64_t nnz_cv) {
+  const int64_t w = dim == 2 ? lsq_width<2>::value : lsq_width<3>::value;
+  // each table starts on a 256-byte boundary (32 doubles)
+  auto up = [](int64_t x) { return (x + 31) / 32 * 32; };
+  return (size_t)(up(w * nc) + up(nnz_cf) + up(dim * nnz_nb) + up(dim * nnz_cv) +
+                  up(2 * dim * nf));
+}
+
 template <int D>
-cudaError_t build_tables(const fvh_mesh_view &m, double *lsq, double *slot_dx) {
-  const int t = 128, nb = (m.num_cells + t - 1) / t;
-  lsq_kernel<D><<<nb, t>>>(m, lsq);
-  slot_dx_kernel<D><<<nb, t>>>(m, slot_dx);
+cudaError_t build_tables(const fvh_mesh_view &m, double *base, int64_t nnz_cf,
+                         int64_t nnz_nb, int64_t nnz_cv, tables *t) {
+  auto up = [](int64_t x) { return (x + 31) / 32 * 32; };
+  double *lsq = base;
+  double *slot_dx = lsq + up((int64_t)lsq_width<D>::value * m.num_cells);
+  double *nbr_dx = slot_dx + up(nnz_cf);
+  double *vtx_dx = nbr_dx + up(D * nnz_nb);
+  double *face_dx = vtx_dx + up(D * nnz_cv);
+  const int th = 128;
+  cell_tables_kernel<D><<<(m.num_cells + th - 1) / th, th>>>(m, lsq, slot_dx, nbr_dx, vtx_dx);
+  face_tables_kernel<D><<<(m.num_faces + th - 1) / th, th>>>(m, face_dx);
+  t->lsq = lsq;
+  t->slot_dx = slot_dx;
+  t->nbr_dx = nbr_dx;
+  t->vtx_dx = vtx_dx;
+  t->face_dx = face_dx;
   return cudaGetLastError();
 }
 
-int lsq_doubles_per_cell(int dim) { return dim == 2 ? lsq_width<2>::value : lsq_width<3>::value; }
-
-template <int D, bool SECOND>
+template <int D, bool SECOND, bool PRE>
 static void launch_fluxes_kind(const fvh_mesh_view &m, const fvh_state_view &s,
                                const fvh_gradient_view &g, const fvh_flux_view &fl,
-                               const fvh_params &p, cudaStream_t st) {
+                               const fvh_params &p, cudaStream_t st, const double *face_dx) {
   const int nb = (m.num_faces + kFaceThreads - 1) / kFaceThreads;
   if (p.flux_kind == FVH_FLUX_RUSANOV)
-    fluxes_kernel<D, FVH_FLUX_RUSANOV, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
+    fluxes_kernel<D, FVH_FLUX_RUSANOV, SECOND, PRE><<<nb, kFaceThreads, 0, st>>>(
+        m, s, g, fl, p.recon_swap_ep, p.boundary, face_dx);
   else if (p.flux_kind == FVH_FLUX_HLLC)
-    fluxes_kernel<D, FVH_FLUX_HLLC, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
+    fluxes_kernel<D, FVH_FLUX_HLLC, SECOND, PRE><<<nb, kFaceThreads, 0, st>>>(
+        m, s, g, fl, p.recon_swap_ep, p.boundary, face_dx);
   else
-    fluxes_kernel<D, FVH_FLUX_HLLE, SECOND><<<nb, kFaceThreads, 0, st>>>(m, s, g, fl, p.recon_swap_ep, p.boundary);
+    fluxes_kernel<D, FVH_FLUX_HLLE, SECOND, PRE><<<nb, kFaceThreads, 0, st>>>(
+        m, s, g, fl, p.recon_swap_ep, p.boundary, face_dx);
 }
 
 template <int D>
 cudaError_t launch_fluxes(const fvh_mesh_view &m, const fvh_state_view &s,
                           const fvh_gradient_view &g, const fvh_flux_view &fl,
-                          const fvh_params &p, cudaStream_t st) {
+                          const fvh_params &p, cudaStream_t st, const tables &t) {
   if (p.order == 1)
-    launch_fluxes_kind<D, false>(m, s, g, fl, p, st);
+    launch_fluxes_kind<D, false, false>(m, s, g, fl, p, st, nullptr);
+  else if (t.face_dx)
+    launch_fluxes_kind<D, true, true>(m, s, g, fl, p, st, t.face_dx);
   else
-    launch_fluxes_kind<D, true>(m, s, g, fl, p, st);
+    launch_fluxes_kind<D, true, false>(m, s, g, fl, p, st, nullptr);
   return cudaGetLastError();
 }
 
@@ -649,11 +993,12 @@ cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const dou
                                     const double *);                                   \
   template cudaError_t launch_gradients<D>(const fvh_mesh_view &, const fvh_state_view &, \
                                            const fvh_gradient_view &, const fvh_params &, \
-                                           cudaStream_t, const double *);              \
-  template cudaError_t build_tables<D>(const fvh_mesh_view &, double *, double *);     \
+                                           cudaStream_t, const tables &);              \
+  template cudaError_t build_tables<D>(const fvh_mesh_view &, double *, int64_t, int64_t, \
+                                       int64_t, tables *);                             \
   template cudaError_t launch_fluxes<D>(const fvh_mesh_view &, const fvh_state_view &, \
                                         const fvh_gradient_view &, const fvh_flux_view &, \
-                                        const fvh_params &, cudaStream_t);             \
+                                        const fvh_params &, cudaStream_t, const tables &); \
   template cudaError_t launch_update<D>(const fvh_mesh_view &, const fvh_params &,     \
                                         const double *, double, const fvh_flux_view &, \
                                         const fvh_state_view &, double *,              \

@@ -17,7 +17,7 @@ _LIB: Optional[C.CDLL] = None
 
 # fvh_status
 OK, ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_INFINITE_DT, ERR_NEGATIVE_STATE = 0, 1, 2, 3, 4
-ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_OUT_OF_MEMORY, ERR_CAPACITY = 5, 6, 7, 8
+ERR_UNSUPPORTED, ERR_NO_DEVICE, ERR_OUT_OF_MEMORY, ERR_CAPACITY, ERR_TIMEOUT = 5, 6, 7, 8, 9
 # fvh_flux_kind / fvh_limiter_kind / fvh_precision
 FLUX = {"hlle": 0, "rusanov": 1, "hllc": 2}
 LIMITER = {"barth_jespersen": 0, "none": 1}
@@ -138,6 +138,7 @@ def _declare(L: C.CDLL) -> None:
         "fvh_solver_set_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
         "fvh_solver_launches_per_run": (C.c_int64, [vp, C.c_int64]),
         "fvh_debug_split": (C.c_int, [vp, C.c_int64, vp, vp, vp, vp, vp]),
+        "fvh_debug_sf64": (C.c_int, [C.c_int32, vp, vp, C.c_int64, vp, vp]),
         "fvh_input_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
         "fvh_input_load_string": (C.c_int, [C.c_char_p, C.c_char_p, C.c_size_t, C.POINTER(vp)]),
         "fvh_input_destroy": (None, [vp]),

@@ -56,7 +56,9 @@ typedef enum fvh_status {
   FVH_ERR_NO_DEVICE = 6,          /* no CUDA device visible                       */
   FVH_ERR_OUT_OF_MEMORY = 7,      /* a device or host allocation failed; no C++
                                      exception ever crosses this ABI            */
-  FVH_ERR_CAPACITY = 8            /* a request exceeds a fixed capacity           */
+  FVH_ERR_CAPACITY = 8,           /* a request exceeds a fixed capacity           */
+  FVH_ERR_TIMEOUT = 9             /* a kernel's bounded wait on its own data
+                                     copies ran out (the kernel stopped early)   */
 } fvh_status;
 
 /* Human-readable text for an fvh_status value (static storage). */
@@ -305,6 +307,16 @@ fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_
  * converted back to FP64.  No reference counterpart. */
 fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, float *rn32,
                            double *hi_as_double, fvh_stream_t stream);
+
+/* Diagnostic of the FP64 kernels' integer-pipe arithmetic on device arrays of
+ * n elements: out[i] = a[i] op b[i], op 0 = multiply, 1 = add, 2 = subtract,
+ * 3 = divide, each correctly rounded to nearest-even on the integer/FP32
+ * pipes; op 4..7 = the same four with the FP64 instructions; op 8 / 9 = the
+ * FP64 kernels' branch-free multiply / divide, redone with the FP64
+ * instruction where they flag an operand.  All must agree bit for bit with
+ * the FP64 instructions on every input.  No reference counterpart. */
+fvh_status fvh_debug_sf64(int32_t op, const double *a, const double *b, int64_t n,
+                          double *out, fvh_stream_t stream);
 
 /* Times each candidate launch shape for trial_steps steps on a scratch copy
  * of `state`, in two interleaved rounds (a shape's figure is its faster
