@@ -321,13 +321,17 @@ static fvh_status solver_step_flags(fvh_solver *s, const fvh_state_view *state, 
 
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule) {
+  const bool staged = (schedule & FVH_SCHEDULE_STAGED) != 0;
+  schedule &= ~FVH_SCHEDULE_STAGED;
   if (!s || (block != 128 && block != 256) || cells_per_thread < 1 || cells_per_thread > 8 ||
       schedule < 0 || schedule > 2 ||
-      (schedule == 2 && fvh::mixed::colours(s->mixed) == 0))
+      (schedule == 2 && fvh::mixed::colours(s->mixed) == 0) ||
+      (staged && !fvh::mixed::staging(s->mixed)))
     return FVH_ERR_INVALID_ARGUMENT;
   s->shape.block = block;
   s->shape.cells_per_thread = cells_per_thread;
   s->shape.schedule = schedule;
+  s->shape.staged = staged;
   drop_graphs(s);
   return FVH_OK;
 }
@@ -392,14 +396,23 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
   cudaEventCreate(&e1);
   // every shape timed in each of kAutotuneRounds interleaved rounds; a shape's
   // figure is its fastest round (robust to a one-off slow trial)
-  constexpr int NS = fvh::mixed::kNumShapes;
-  double shape_ms[NS];
+  // each shape with the global-memory gradients, and where the mesh allows
+  // it with the staged ones
+  constexpr int NB = fvh::mixed::kNumShapes;
+  const int NS = fvh::mixed::staging(s->mixed) ? 2 * NB : NB;
+  auto shape_at = [&](int i) {
+    fvh::mixed::launch_shape c = fvh::mixed::kShapes[i % NB];
+    c.staged = i >= NB;
+    return c;
+  };
+  double shape_ms[2 * NB];
   for (int i = 0; i < NS; ++i) shape_ms[i] = -1;
   for (int round = 0; round < fvh::mixed::kAutotuneRounds; ++round) {
     for (int i = 0; i < NS; ++i) {
-      const auto &c = fvh::mixed::kShapes[i];
+      const auto c = shape_at(i);
       if (e != cudaSuccess) break;
-      fvh_solver_set_shape(s, c.block, c.cells_per_thread, c.schedule);
+      fvh_solver_set_shape(s, c.block, c.cells_per_thread,
+                           c.schedule | (c.staged ? FVH_SCHEDULE_STAGED : 0));
       refresh();
       // timed as fvh_solver_run launches steps
       fvh_status r = FVH_OK;
@@ -421,7 +434,7 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
   for (int i = 0; i < NS; ++i)
     if (shape_ms[i] >= 0 && (best_ms < 0 || shape_ms[i] < best_ms)) {
       best_ms = shape_ms[i];
-      best = fvh::mixed::kShapes[i];
+      best = shape_at(i);
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -432,11 +445,12 @@ fvh_status fvh_solver_autotune(fvh_solver *s, const fvh_state_view *state, int32
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFree(scratch);
   cudaFree(saved_t);
-  fvh_solver_set_shape(s, best.block, best.cells_per_thread, best.schedule);
+  fvh_solver_set_shape(s, best.block, best.cells_per_thread,
+                       best.schedule | (best.staged ? FVH_SCHEDULE_STAGED : 0));
   if (e != cudaSuccess) return from_cuda(e);
   if (block) *block = best.block;
   if (cells_per_thread) *cells_per_thread = best.cells_per_thread;
-  if (schedule) *schedule = best.schedule;
+  if (schedule) *schedule = best.schedule | (best.staged ? FVH_SCHEDULE_STAGED : 0);
   if (best_ms_per_step) *best_ms_per_step = best_ms;
   return FVH_OK;
 }

@@ -943,7 +943,7 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 constexpr int kStageCells = 128;     // cells per chunk = threads per block
 constexpr int kStageMaxCells = 256;  // staged cell records per chunk
 constexpr int kStageMaxVerts = 224;  // staged vertex records per chunk
-constexpr int kStageTopoBytes = 5120;
+constexpr int kStageTopoBytes = 3072;
 constexpr int kStagePackBytes = kStageMaxCells * 32;
 constexpr int kStageCenBytes = kStageMaxCells * 16;
 constexpr int kStageVtxBytes = kStageMaxVerts * 16;
@@ -1016,15 +1016,6 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
     const int k = chunk_at(i);
     const int c0 = t.cells[(size_t)k * kStageCells + tid];
     const bool landed = tma::mbar_wait_bounded(&bar[b], (unsigned)(used[b] & 1), kStageWaitPolls);
-    if (__syncthreads_or(!landed)) {
-      // report, then wait (bounded) for every posted copy before leaving, so
-      // none lands in shared memory this block no longer owns
-      if (tid == 0) atomicMin(status, status_key(t.cells[(size_t)k * kStageCells], FVH_ERR_TIMEOUT));
-      for (int bb = 0; bb < 2; ++bb)
-        if (posted[bb] > used[bb])
-          tma::mbar_wait_bounded(&bar[bb], (unsigned)((posted[bb] - 1) & 1), kStageWaitPolls);
-      return;
-    }
     ++used[b];
     const unsigned char *base = smem + (size_t)b * kStageBytes;
     const float4 *spk = reinterpret_cast<const float4 *>(base);
@@ -1032,10 +1023,10 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
     const float4 *svtx = reinterpret_cast<const float4 *>(base + kStagePackBytes + kStageCenBytes);
     const unsigned short *topo = reinterpret_cast<const unsigned short *>(
         base + kStagePackBytes + kStageCenBytes + kStageVtxBytes);
-    if (c0 >= 0) {
-      const unsigned short *rec = topo + topo[tid];
+    if (landed && c0 >= 0) {
+      const unsigned char *rec = reinterpret_cast<const unsigned char *>(topo) + topo[tid];
       const int own = rec[0], nn = rec[1], nr = rec[2];
-      const unsigned short *nslot = rec + 3, *vslot = rec + 3 + nn;
+      const unsigned char *nslot = rec + 3, *vslot = rec + 3 + nn;
       const float4 a0 = spk[2 * own], b0 = spk[2 * own + 1];
       const float4 x0 = scen[own];
       const float xh[3] = {x0.x, x0.y, 0.f}, xl[3] = {x0.z, x0.w, 0.f};
@@ -1054,7 +1045,18 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
             vh[0] = v.x; vh[1] = v.y; vl[0] = v.z; vl[1] = v.w;
           });
     }
-    __syncthreads();
+    // the one block barrier of a chunk: every thread is done with this
+    // buffer before it is posted again, and a wait that ran out anywhere
+    // stops the whole block
+    if (__syncthreads_or(!landed)) {
+      // report, then wait (bounded) for every posted copy before leaving, so
+      // none lands in shared memory this block no longer owns
+      if (tid == 0) atomicMin(status, status_key(t.cells[(size_t)k * kStageCells], FVH_ERR_TIMEOUT));
+      for (int bb = 0; bb < 2; ++bb)  // (a phase that completed returns at once)
+        if (posted[bb] > 0)
+          tma::mbar_wait_bounded(&bar[bb], (unsigned)((posted[bb] - 1) & 1), kStageWaitPolls);
+      return;
+    }
   }
 }
 
@@ -1681,15 +1683,18 @@ static cudaError_t setup_colours_host(workspace *w, const fvh_mesh_view &m) {
   return e;
 }
 
+bool staging(const workspace *w) { return w && w->stage.nchunks > 0; }
+
 int colours(const workspace *w) { return w ? w->ncolours : 0; }
 
 // Tables of the staged 2D gradients (see gradients_staged_kernel), built on
 // the host from the mesh.  Chunks: kStageCells consecutive cells of the Morton
 // order of the centroids (16-bit quantised coordinates, bits interleaved).
-// Per chunk, a topology block of 16-bit words: word i (i < kStageCells) is the
-// start of cell i's record (or 0xffff), a record is (own slot, number of
-// neighbours nn, number of vertices nr, nn neighbour slots, nr vertex slots);
-// the block is padded to 16 bytes.  A mesh with a chunk whose staged set or
+// Per chunk, a topology block: 16-bit word i (i < kStageCells) is the byte
+// offset of cell i's record (or 0xffff), a record is bytes (own slot, number
+// of neighbours nn, number of vertices nr, nn neighbour slots, nr vertex
+// slots) -- a chunk stages at most 256 cell and vertex records, so a slot
+// fits in a byte; the block is padded to 16 bytes.  A mesh with a chunk whose staged set or
 // topology does not fit keeps the global-memory kernel (nchunks stays 0).
 static unsigned spread_bits16(unsigned x) {
   x &= 0xffffu;
@@ -1768,20 +1773,29 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
     auto pos = [](const std::vector<int> &v, int x) {
       return (unsigned short)(std::lower_bound(v.begin(), v.end(), x) - v.begin());
     };
-    std::vector<unsigned short> &tb = topo[k];
-    tb.assign(kStageCells, 0xffffu);
-    for (int i = i0; i < i1; ++i) {
+    std::vector<unsigned char> bytes;
+    std::vector<unsigned short> index(kStageCells, 0xffffu);
+    bool ok = true;
+    for (int i = i0; i < i1 && ok; ++i) {
       const int c = order[i].second;
-      tb[i - i0] = (unsigned short)tb.size();
-      tb.push_back(pos(ids, c));
-      tb.push_back((unsigned short)(nb_off[c + 1] - nb_off[c]));
-      tb.push_back((unsigned short)(cv_off[c + 1] - cv_off[c]));
-      for (int q = nb_off[c]; q < nb_off[c + 1]; ++q) tb.push_back(pos(ids, nb[q]));
-      for (int r = cv_off[c]; r < cv_off[c + 1]; ++r) tb.push_back(pos(vids, cv[r]));
-      if (tb.size() > 0xffffu) break;
+      const int nn = nb_off[c + 1] - nb_off[c], nr = cv_off[c + 1] - cv_off[c];
+      ok = nn < 256 && nr < 256;
+      index[i - i0] = (unsigned short)(2 * kStageCells + bytes.size());
+      bytes.push_back((unsigned char)pos(ids, c));
+      bytes.push_back((unsigned char)nn);
+      bytes.push_back((unsigned char)nr);
+      for (int q = nb_off[c]; q < nb_off[c + 1]; ++q) bytes.push_back((unsigned char)pos(ids, nb[q]));
+      for (int r = cv_off[c]; r < cv_off[c + 1]; ++r) bytes.push_back((unsigned char)pos(vids, cv[r]));
     }
-    while (tb.size() % 8) tb.push_back(0);  // 16-byte multiple
-    if (tb.size() * 2 > (size_t)kStageTopoBytes) fits = 0;
+    while (bytes.size() % 16) bytes.push_back(0);  // 16-byte multiple
+    if (!ok || 2 * kStageCells + bytes.size() > (size_t)kStageTopoBytes) {
+      fits = 0;
+      continue;
+    }
+    std::vector<unsigned short> &tb = topo[k];
+    tb = index;
+    for (size_t j = 0; j < bytes.size(); j += 2)
+      tb.push_back((unsigned short)(bytes[j] | (bytes[j + 1] << 8)));
   }
   if (!fits) return cudaSuccess;  // the global-memory kernel serves this mesh
   std::vector<int> cells((size_t)nchunks * kStageCells, -1);
@@ -1883,7 +1897,8 @@ template <int D, int KIND, bool SECOND, int BS>
 // L2).  Results do not depend on the order.
 static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_params &p,
                             const fvh_state_view &s, const problem_map &pm, int stage,
-                            int cpt, int schedule, cudaStream_t st, const launch_mark &mark,
+                            int cpt, int schedule, bool staged, cudaStream_t st,
+                            const launch_mark &mark,
                             int &dir, const next_dt *nd) {
   const long long per = (long long)BS * cpt;
   const int nb = (int)((m.num_cells + per - 1) / per);
@@ -1897,7 +1912,7 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
   const int nb_next = nb < kCflMaxBlocks ? nb : kCflMaxBlocks;
   if (SECOND) {
     dir ^= 1;
-    if (D == 2 && w->stage.nchunks > 0 && !pm.cell_problem) {
+    if (D == 2 && staged && w->stage.nchunks > 0 && !pm.cell_problem) {
       const int smem = 2 * kStageBytes;
       if (p.limiter == FVH_LIMITER_NONE)
         gradients_staged_kernel<false><<<w->stage_blocks, kStageCells, smem, st>>>(
@@ -1987,10 +2002,10 @@ static void launch_stage(workspace *w, const fvh_mesh_view &m, const fvh_params 
                          int &dir, const next_dt *nd) {
   if (sh.block == 256)
     launch_stage_bs<D, KIND, SECOND, 256>(w, m, p, s, pm, stage, sh.cells_per_thread,
-                                          sh.schedule, st, mark, dir, nd);
+                                          sh.schedule, sh.staged, st, mark, dir, nd);
   else
     launch_stage_bs<D, KIND, SECOND, 128>(w, m, p, s, pm, stage, sh.cells_per_thread,
-                                          sh.schedule, st, mark, dir, nd);
+                                          sh.schedule, sh.staged, st, mark, dir, nd);
 }
 
 template <int D, int KIND>

@@ -35,6 +35,9 @@ struct launch_mark {
 struct launch_shape {
   int block = 128;          // threads per block: 128 or 256
   int cells_per_thread = 1; // grid = ceil(cells / (block * cells_per_thread)), grid-stride
+  bool staged = false;      // 2D single mesh: gradients from records staged in shared
+                            // memory by the bulk-copy engine (gradients_staged_kernel);
+                            // the same bits as the global-memory gather
   int schedule = 0;         // 0: cell-centric (each cell evaluates its faces' fluxes);
                             // 1: one flux per face into an array, then a cell gather;
                             // 2: face colouring (single mesh only): per colour, one
@@ -43,15 +46,19 @@ struct launch_shape {
 
 // Candidate shapes the autotuners time (the batch form skips schedule 2).
 constexpr int kNumShapes = 9;
-constexpr launch_shape kShapes[kNumShapes] = {{128, 1, 0}, {256, 1, 0}, {128, 2, 0},
-                                              {256, 2, 0}, {128, 1, 1}, {256, 1, 1},
-                                              {128, 2, 1}, {128, 1, 2}, {256, 1, 2}};
+constexpr launch_shape kShapes[kNumShapes] = {
+    {128, 1, false, 0}, {256, 1, false, 0}, {128, 2, false, 0}, {256, 2, false, 0},
+    {128, 1, false, 1}, {256, 1, false, 1}, {128, 2, false, 1}, {128, 1, false, 2},
+    {256, 1, false, 2}};
 // Interleaved timing rounds per shape in the autotuners (each shape keeps its
 // fastest round).
 constexpr int kAutotuneRounds = 2;
 
 // Number of face colours of a workspace made by create() (0 for the batch's).
 int colours(const workspace *w);
+// Whether the staged gradients serve this workspace's mesh (2D single mesh
+// whose chunks fit the shared-memory stages).
+bool staging(const workspace *w);
 
 // Steps of one run on a state nothing else writes in between: the corrector
 // of a step can also write the next step's FP32 pack and dt (the same bits

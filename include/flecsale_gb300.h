@@ -296,8 +296,12 @@ int32_t fvh_solver_launches_per_step(const fvh_solver *s);
  * cell, one flux per face added to its cells' compensated sums; then the
  * update).  Schedules 0 and 1 and all block sizes / cells per thread give the
  * same bits; schedule 2 adds each cell's fluxes in colour order, so its sums
- * round differently (deterministically).  The FP64 form ignores it.  No
+ * round differently (deterministically).  schedule | FVH_SCHEDULE_STAGED (2D
+ * meshes whose cell chunks fit the stages; FVH_ERR_INVALID_ARGUMENT otherwise)
+ * takes the gradients from neighbour records staged in shared memory by the
+ * bulk-copy engine, with the same bits.  The FP64 form ignores it.  No
  * reference counterpart: the reference's tasks have no launch configuration. */
+#define FVH_SCHEDULE_STAGED 4
 fvh_status fvh_solver_set_shape(fvh_solver *s, int32_t block, int32_t cells_per_thread,
                                 int32_t schedule);
 
@@ -318,8 +322,9 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
 fvh_status fvh_debug_sf64(int32_t op, const double *a, const double *b, int64_t n,
                           double *out, fvh_stream_t stream);
 
-/* Times each candidate launch shape for trial_steps steps on a scratch copy
- * of `state`, in two interleaved rounds (a shape's figure is its faster
+/* Times each candidate launch shape (with and without FVH_SCHEDULE_STAGED
+ * where the mesh allows it) for trial_steps steps on a scratch copy of
+ * `state`, in two interleaved rounds (a shape's figure is its faster
  * round), and keeps the fastest; the state, solution time and status word are
  * left unchanged.  Synchronises; allocates the scratch copy.  No reference
  * counterpart. */
