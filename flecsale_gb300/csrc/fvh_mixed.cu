@@ -77,6 +77,7 @@ struct stage_tables {
   const int *run_off = nullptr;              // [nchunks + 1] into runs
   const stage_run *runs = nullptr;
   const long long *topo_off = nullptr;       // [nchunks + 1] byte offsets into topo
+  const unsigned *bytes = nullptr;           // [nchunks] bytes staged per chunk
   const unsigned short *topo = nullptr;      // per chunk: see setup_stage_host
 };
 
@@ -588,9 +589,6 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
                                                const float *xl, int nn, NBR nbr) {
   constexpr int NV = D + 4;
   constexpr float tol = 1.e-9f;
-  float umin[NV], umax[NV];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
   float M[6] = {0, 0, 0, 0, 0, 0};
   float b[NV][D];
 #pragma unroll
@@ -617,8 +615,6 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      umin[k] = fminf(u1[k], umin[k]);
-      umax[k] = fmaxf(u1[k], umax[k]);
       const float du = u1[k] - u0[k];
 #pragma unroll
       for (int j = 0; j < D; ++j) b[k][j] += du * dx[j];
@@ -672,6 +668,27 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
       for (int i = 0; i < D; ++i) dxv[i] = __fadd_rn(__fsub_rn(vh[i], xh[i]), __fsub_rn(vl[i], xl[i]));
       vertex(dxv);
     }
+    // the neighbour extrema (tasks.h:232-236) only when some variable can be
+    // limited: a second pass over the neighbours (min / max do not depend on
+    // the order, so the values are those of a single pass)
+    float umin[NV], umax[NV];
+    bool need = false;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      umin[k] = umax[k] = u0[k];
+      need = need || dpos[k] > tol || dneg[k] < -tol;
+    }
+    if (need) {
+      for (int q = 0; q < nn; ++q) {
+        float u1[NV], yh[3], yl[3];
+        nbr(q, u1, yh, yl);
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          umin[k] = fminf(u1[k], umin[k]);
+          umax[k] = fmaxf(u1[k], umax[k]);
+        }
+      }
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       float phi = 1.f;
@@ -721,12 +738,6 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
   constexpr int NP = NV / 2;      // slot pairs; 3D has slot NV-1 (a) left over
   constexpr bool ODD = NV % 2 == 1;
   constexpr float tol = 1.e-9f;
-  float umin[NV], umax[NV];
-  {
-    const float u0[8] = {a0.x, a0.y, a0.z, a0.w, b0.x, b0.y, b0.z, b0.w};
-#pragma unroll
-    for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
-  }
   // -u0 by slot (u_q - u0 = u_q + (-u0) exactly)
   const float nu0s[8] = {-a0.x, -a0.y, -a0.z, -a0.w, -b0.x, -b0.y, -b0.z, -b0.w};
   float2 nu0[NP];
@@ -759,12 +770,6 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
       mB = fma2(dx01, bcast(dx[2]), mB);
       m22 += dx[2] * dx[2];
     }
-    const float u1[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      umin[k] = fminf(u1[k], umin[k]);
-      umax[k] = fmaxf(u1[k], umax[k]);
-    }
     const float2 pr[4] = {make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y),
                           make_float2(b.z, b.w)};
 #pragma unroll
@@ -774,6 +779,7 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
       for (int j = 0; j < D; ++j) bs[p][j] = fma2(du, bcast(dx[j]), bs[p][j]);
     }
     if (ODD) {
+      const float u1[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
       const float du = u1[NV - 1] + nu0s[NV - 1];
 #pragma unroll
       for (int j = 0; j < D; ++j) bo[j] += du * dx[j];
@@ -840,6 +846,32 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
         for (int i = 1; i < D; ++i) du += go[i] * dxv[i];
         dpos[NV - 1] = fmaxf(du, dpos[NV - 1]);
         dneg[NV - 1] = fminf(du, dneg[NV - 1]);
+      }
+    }
+    // the neighbour extrema (tasks.h:232-236) only when some variable can be
+    // limited: a second pass over the neighbours (min / max do not depend on
+    // the order, so the values are those of a single pass)
+    float umin[NV], umax[NV];
+    bool need = false;
+    {
+      const float u0[8] = {a0.x, a0.y, a0.z, a0.w, b0.x, b0.y, b0.z, b0.w};
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        umin[k] = umax[k] = u0[k];
+        need = need || dpos[k] > tol || dneg[k] < -tol;
+      }
+    }
+    if (need) {
+      for (int q = 0; q < nn; ++q) {
+        float4 a, b;
+        float yh[3], yl[3];
+        nbr(q, a, b, yh, yl);
+        const float u1[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          umin[k] = fminf(u1[k], umin[k]);
+          umax[k] = fmaxf(u1[k], umax[k]);
+        }
       }
     }
     float phi[NV];
@@ -942,8 +974,8 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 // the same bits.
 constexpr int kStageCells = 128;     // cells per chunk = threads per block
 constexpr int kStageMaxCells = 256;  // staged cell records per chunk
-constexpr int kStageMaxVerts = 224;  // staged vertex records per chunk
-constexpr int kStageTopoBytes = 3072;
+constexpr int kStageMaxVerts = 192;  // staged vertex records per chunk
+constexpr int kStageTopoBytes = 2816;
 constexpr int kStagePackBytes = kStageMaxCells * 32;
 constexpr int kStageCenBytes = kStageMaxCells * 16;
 constexpr int kStageVtxBytes = kStageMaxVerts * 16;
@@ -968,12 +1000,7 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
     // the copies that overwrite it
     tma::fence_proxy_async_shared();
     if (tid == 0) {
-      unsigned bytes = topo_bytes;
-      for (int r = 0; r < nr; ++r) {
-        const stage_run run = t.runs[r0 + r];
-        bytes += (unsigned)run.count * (run.kind == 0 ? 48u : 16u);
-      }
-      tma::mbar_arrive_expect_tx(&bar[b], bytes);
+      tma::mbar_arrive_expect_tx(&bar[b], t.bytes[k]);
       tma::bulk_g2s(base + kStagePackBytes + kStageCenBytes + kStageVtxBytes,
                     reinterpret_cast<const unsigned char *>(t.topo) + tb0, topo_bytes, &bar[b]);
     }
@@ -1802,9 +1829,12 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
   for (int i = 0; i < nc; ++i) cells[i] = order[i].second;
   std::vector<int> run_off(nchunks + 1, 0);
   std::vector<long long> topo_off(nchunks + 1, 0);
+  std::vector<unsigned> chunk_bytes(nchunks, 0);
   for (int k = 0; k < nchunks; ++k) {
     run_off[k + 1] = run_off[k] + (int)runs[k].size();
     topo_off[k + 1] = topo_off[k] + 2 * (long long)topo[k].size();
+    chunk_bytes[k] = 2 * (unsigned)topo[k].size();
+    for (const stage_run &r : runs[k]) chunk_bytes[k] += (unsigned)r.count * (r.kind == 0 ? 48u : 16u);
   }
   std::vector<stage_run> all(run_off[nchunks]);
   std::vector<unsigned short> blob(topo_off[nchunks] / 2);
@@ -1816,9 +1846,10 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
   const size_t b_cells = up(sizeof(int) * cells.size()), b_off = up(sizeof(int) * run_off.size()),
                b_runs = up(sizeof(stage_run) * all.size()),
                b_toff = up(sizeof(long long) * topo_off.size()),
-               b_topo = up(sizeof(unsigned short) * blob.size());
+               b_topo = up(sizeof(unsigned short) * blob.size()),
+               b_bytes = up(sizeof(unsigned) * chunk_bytes.size());
   char *base = nullptr;
-  e = cudaMalloc(&base, b_cells + b_off + b_runs + b_toff + b_topo);
+  e = cudaMalloc(&base, b_cells + b_off + b_runs + b_toff + b_topo + b_bytes);
   if (e != cudaSuccess) return e;
   w->stage_base = base;
   char *p = base;
@@ -1837,6 +1868,8 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
       put(topo_off.data(), sizeof(long long) * topo_off.size(), b_toff));
   t.topo = reinterpret_cast<const unsigned short *>(
       put(blob.data(), sizeof(unsigned short) * blob.size(), b_topo));
+  t.bytes = reinterpret_cast<const unsigned *>(
+      put(chunk_bytes.data(), sizeof(unsigned) * chunk_bytes.size(), b_bytes));
   if (e != cudaSuccess) return e;
   // persistent grid: the blocks that fit on the device at once
   const int smem = 2 * kStageBytes;
