@@ -620,10 +620,10 @@ def run_ours(args):
     E = lambda s: s[0] * (s[3] + 0.5 * (s[1] ** 2 + s[2] ** 2))
 
     def e2e(form):
-        if form == "fp64":  # upload of the 7 planes, steps, download of the 7 planes
-            bi, bo = 7 * 8 * nc, 7 * 8 * nc
-            call = ("fvh_solver_advance_host (pinned host state: 7 planes copied in, 1 step, "
-                    "7 planes copied out)")
+        if form == "fp64":  # 6 planes copied up (not T), the last update writes all 7
+            bi, bo = 6 * 8 * nc, 7 * 8 * nc
+            call = ("fvh_solver_advance_host (pinned host state: the 6 planes the step reads "
+                    "copied in, 1 step; the last update writes the 7 planes to host memory)")
         else:  # the step reads d, v, e, p, a from the host planes and writes all 7
             bi, bo = 6 * 8 * nc, 7 * 8 * nc
             call = ("fvh_solver_advance_host (pinned host state in, 1 step, host state out; the "

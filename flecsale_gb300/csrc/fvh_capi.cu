@@ -300,7 +300,13 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
                         ? fvh::plain::launch_fluxes<2>(m, *state, s->grads, s->flux, p, st, s->tab)
                         : fvh::plain::launch_fluxes<3>(m, *state, s->grads, s->flux, p, st, s->tab));
     mark("fluxes");
-    if (r == FVH_OK) r = fvh_apply_update(&m, &p, dt, 0.5, &s->flux, state, t, s->status, fs);
+    // the last stage of the step may also write the new state to f.out
+    const fvh_state_view *out = stage == 1 ? f.out : nullptr;
+    if (r == FVH_OK)
+      r = from_cuda(m.dim == 2 ? fvh::plain::launch_update<2>(m, p, dt, 0.5, s->flux, *state, t,
+                                                              s->status, st, out)
+                               : fvh::plain::launch_update<3>(m, p, dt, 0.5, s->flux, *state, t,
+                                                              s->status, st, out));
     mark("update");
   }
   return r;
@@ -815,14 +821,14 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
   cudaError_t e = cudaMemcpyAsync(s->scalars, s->host_scalars + 1, sizeof(double),
                                   cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return from_cuda(e);
-  // Pinned (device-mapped) host planes and the mixed form: the first pack_dt
-  // reads the state straight from host memory (storing it into the device
-  // state as it goes) and the last corrector writes the new state back to host
-  // memory while it computes, so the transfers overlap the kernels instead of
-  // preceding and following them.
+  // Pinned (device-mapped) host planes: the last update writes the new state
+  // back to host memory while it computes, so the download overlaps the kernel
+  // instead of following it.  In the mixed form the first pack_dt also reads
+  // the state straight from host memory (storing it into the device state as
+  // it goes); in the FP64 form the planes the step reads are copied up first,
+  // all but the temperature, which no kernel reads and the update rewrites.
   cudaPointerAttributes attr{};
-  if (nsteps > 0 && s->params.precision == FVH_PRECISION_MIXED &&
-      cudaPointerGetAttributes(&attr, host_planes) == cudaSuccess &&
+  if (nsteps > 0 && cudaPointerGetAttributes(&attr, host_planes) == cudaSuccess &&
       attr.type == cudaMemoryTypeHost && attr.devicePointer) {
     double *hp = static_cast<double *>(attr.devicePointer);
     fvh_state_view hv{};
@@ -834,9 +840,18 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
     hv.temperature = hp + (size_t)k++ * nc;
     hv.sound_speed = hp + (size_t)k++ * nc;
     fvh_status r = FVH_OK;
+    const bool mixed = s->params.precision == FVH_PRECISION_MIXED;
+    if (!mixed) {
+      double *dp[9];
+      state_planes(dev_state, D, dp);
+      for (int k = 0; k < 5 + D && r == FVH_OK; ++k)
+        if (k != D + 3)  // temperature
+          r = from_cuda(cudaMemcpyAsync(dp[k], host_planes + (size_t)k * nc, sizeof(double) * nc,
+                                        cudaMemcpyHostToDevice, st));
+    }
     for (int64_t n = 0; n < nsteps && r == FVH_OK; ++n) {
       fvh::mixed::step_flags f = chunk_flags(n, nsteps);
-      if (n == 0) f.src = &hv;
+      if (mixed && n == 0) f.src = &hv;
       if (n + 1 == nsteps) f.out = &hv;
       r = solver_step_enqueue(s, dev_state, st, {}, f);
     }

@@ -84,11 +84,14 @@ cudaError_t launch_fluxes(const fvh_mesh_view &m, const fvh_state_view &s,
 // 8 / 9 the optimistic mul / div with their FP64 redo.
 cudaError_t debug_sf64(int op, const double *a, const double *b, int64_t n, double *out,
                        cudaStream_t st);
+// out (optional): a second copy of the new state, e.g. host-mapped planes of
+// a caller that holds its state in host memory
 template <int D>
 cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const double *dt,
                           double factor, const fvh_flux_view &fl,
                           const fvh_state_view &s, double *soln_time,
-                          fvh_device_status *status, cudaStream_t st);
+                          fvh_device_status *status, cudaStream_t st,
+                          const fvh_state_view *out = nullptr);
 }  // namespace plain
 
 }  // namespace fvh

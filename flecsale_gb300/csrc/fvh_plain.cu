@@ -824,7 +824,8 @@ template <int D>
 __global__ void __launch_bounds__(kCellThreads)
 update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_view s,
               const double *dt, double factor, double gm1, double ggm1, double cv,
-              double *soln_time, fvh_device_status *status) {
+              double *soln_time, fvh_device_status *status, const fvh_state_view out,
+              int has_out) {
   const double delta_t = __dmul_rn(dt[0], factor);
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c == 0) soln_time[0] = 0.0 + soln_time[0] + delta_t;
@@ -838,13 +839,23 @@ update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_vie
       cell_update<D>(hw, m, fl, s, c, delta_t, gm1, ggm1, cv, w);
     }
   }
+  const double a = sqrt(w[D + 4]);
   s.density[c] = w[0];
 #pragma unroll
   for (int i = 0; i < D; ++i) s.velocity[i][c] = w[1 + i];
   s.internal_energy[c] = w[D + 1];
   s.pressure[c] = w[D + 2];
   s.temperature[c] = w[D + 3];
-  s.sound_speed[c] = sqrt(w[D + 4]);
+  s.sound_speed[c] = a;
+  if (has_out) {
+    out.density[c] = w[0];
+#pragma unroll
+    for (int i = 0; i < D; ++i) out.velocity[i][c] = w[1 + i];
+    out.internal_energy[c] = w[D + 1];
+    out.pressure[c] = w[D + 2];
+    out.temperature[c] = w[D + 3];
+    out.sound_speed[c] = a;
+  }
   if (lt0(w[D + 1]) || lt0(w[0])) atomicMin(status, status_key(c, FVH_ERR_NEGATIVE_STATE));
 }
 
@@ -986,14 +997,15 @@ template <int D>
 cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const double *dt,
                           double factor, const fvh_flux_view &fl,
                           const fvh_state_view &s, double *soln_time,
-                          fvh_device_status *status, cudaStream_t st) {
+                          fvh_device_status *status, cudaStream_t st,
+                          const fvh_state_view *out) {
   const int nb = (m.num_cells + kCellThreads - 1) / kCellThreads;
   // the same two roundings as (gamma - 1.0) and gamma * (gamma - 1.0) per cell
   const double gamma = p.gamma;
   const double gm1 = gamma - 1.0;
   const double ggm1 = gamma * gm1;
   update_kernel<D><<<nb, kCellThreads, 0, st>>>(m, fl, s, dt, factor, gm1, ggm1, p.cv,
-                                                soln_time, status);
+                                                soln_time, status, out ? *out : s, out ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -1013,7 +1025,8 @@ cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const dou
   template cudaError_t launch_update<D>(const fvh_mesh_view &, const fvh_params &,     \
                                         const double *, double, const fvh_flux_view &, \
                                         const fvh_state_view &, double *,              \
-                                        fvh_device_status *, cudaStream_t);
+                                        fvh_device_status *, cudaStream_t,             \
+                                        const fvh_state_view *);
 FVH_INSTANTIATE(2)
 FVH_INSTANTIATE(3)
 
