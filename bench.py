@@ -445,9 +445,11 @@ def run_serving(torch, stream, batched_rate: float, seconds: float, seed: int = 
     return rep
 
 
-def run_3d(torch, stream, n: int = 192, steps: int = 100) -> dict:
+def run_3d(torch, stream, n: int = 192, steps: int = 100, shape: str = "") -> dict:
     """192^3 hex shock box (inner cube [0,0.5]^3 at rho=1,p=1, rest 0.125/0.1),
-    jitter +-0.15h (seed 2), Rusanov, CFL 0.3, 100 steps: FP64 vs mixed."""
+    jitter +-0.15h (seed 2), Rusanov, CFL 0.3, 100 steps: FP64 vs mixed.  The
+    mixed form's launch shape is autotuned unless `shape` ("block,cpt,schedule")
+    fixes it."""
     import flecsale_gb300.hydro as H
     t0 = time.perf_counter()
     mesh = H.HostMesh.box(3, (n, n, n), [0, 0, 0], [1, 1, 1], 0.15, 2)
@@ -463,7 +465,12 @@ def run_3d(torch, stream, n: int = 192, steps: int = 100) -> dict:
         sv = H.Solver(dm, p)
         ds.upload(s0, stream)
         sv.reset(0.0, stream)
-        if form == "mixed":
+        if form == "mixed" and shape:
+            blk, cpt, sch = (int(v) for v in shape.split(","))
+            sv.set_shape(blk, cpt, sch)
+            out["mixed_launch_shape"] = {"block": blk, "cells_per_thread": cpt,
+                                         "schedule": sch, "fixed": True}
+        elif form == "mixed":
             out["mixed_launch_shape"] = sv.autotune(ds, 3, stream)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -761,7 +768,8 @@ def main():
     if args.only_3d:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps(run_3d(torch, torch.cuda.Stream(), args.only_3d, args.steps)), flush=True)
+        print(json.dumps(run_3d(torch, torch.cuda.Stream(), args.only_3d, args.steps,
+                                args.shape)), flush=True)
         return 0
     if args.only_2d:
         return run_only_2d(args)
