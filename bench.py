@@ -627,14 +627,12 @@ def run_ours(args):
     E = lambda s: s[0] * (s[3] + 0.5 * (s[1] ** 2 + s[2] ** 2))
 
     def e2e(form):
-        if form == "fp64":  # 6 planes copied up (not T), the last update writes all 7
-            bi, bo = 6 * 8 * nc, 7 * 8 * nc
-            call = ("fvh_solver_advance_host (pinned host state: the 6 planes the step reads "
-                    "copied in, 1 step; the last update writes the 7 planes to host memory)")
-        else:  # the step reads d, v, e, p, a from the host planes and writes all 7
-            bi, bo = 6 * 8 * nc, 7 * 8 * nc
-            call = ("fvh_solver_advance_host (pinned host state in, 1 step, host state out; the "
-                    "first and last kernels access the host planes directly)")
+        # the step reads d, v, e, p, a from the host planes and writes all 7
+        bi, bo = 6 * 8 * nc, 7 * 8 * nc
+        first = "dt" if form == "fp64" else "pack_dt"
+        call = (f"fvh_solver_advance_host (pinned host state in, 1 step, host state out; the "
+                f"first kernel ({first}) reads and the last update writes the host planes "
+                "directly)")
         return {"value": ws * nc * args.steps / results[form]["e2e_s"], "unit": UNIT,
                 "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "call": call}
 

@@ -284,8 +284,10 @@ static fvh_status solver_step_enqueue(fvh_solver *s, const fvh_state_view *state
   const fvh_stream_t fs = reinterpret_cast<fvh_stream_t>(st);
   const int nb = dt_blocks(m.num_cells);
   fvh_status r = from_cuda(
-      m.dim == 2 ? fvh::plain::launch_dt<2>(m, *state, p, t, dt, partial, nb, s->status, st, s->tab.slot_dx)
-                 : fvh::plain::launch_dt<3>(m, *state, p, t, dt, partial, nb, s->status, st, s->tab.slot_dx));
+      m.dim == 2 ? fvh::plain::launch_dt<2>(m, *state, p, t, dt, partial, nb, s->status, st,
+                                            s->tab.slot_dx, f.src)
+                 : fvh::plain::launch_dt<3>(m, *state, p, t, dt, partial, nb, s->status, st,
+                                            s->tab.slot_dx, f.src));
   mark("dt");
   for (int stage = 0; stage < 2 && r == FVH_OK; ++stage) {
     if (p.order == 1)
@@ -821,12 +823,11 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
   cudaError_t e = cudaMemcpyAsync(s->scalars, s->host_scalars + 1, sizeof(double),
                                   cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return from_cuda(e);
-  // Pinned (device-mapped) host planes: the last update writes the new state
-  // back to host memory while it computes, so the download overlaps the kernel
-  // instead of following it.  In the mixed form the first pack_dt also reads
-  // the state straight from host memory (storing it into the device state as
-  // it goes); in the FP64 form the planes the step reads are copied up first,
-  // all but the temperature, which no kernel reads and the update rewrites.
+  // Pinned (device-mapped) host planes: the first kernel (the mixed form's
+  // pack_dt, the FP64 form's dt) reads the state straight from host memory,
+  // storing it into the device state as it goes, and the last update writes
+  // the new state back to host memory while it computes, so the transfers
+  // overlap the kernels instead of preceding and following them.
   cudaPointerAttributes attr{};
   if (nsteps > 0 && cudaPointerGetAttributes(&attr, host_planes) == cudaSuccess &&
       attr.type == cudaMemoryTypeHost && attr.devicePointer) {
@@ -840,18 +841,9 @@ fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_stat
     hv.temperature = hp + (size_t)k++ * nc;
     hv.sound_speed = hp + (size_t)k++ * nc;
     fvh_status r = FVH_OK;
-    const bool mixed = s->params.precision == FVH_PRECISION_MIXED;
-    if (!mixed) {
-      double *dp[9];
-      state_planes(dev_state, D, dp);
-      for (int k = 0; k < 5 + D && r == FVH_OK; ++k)
-        if (k != D + 3)  // temperature
-          r = from_cuda(cudaMemcpyAsync(dp[k], host_planes + (size_t)k * nc, sizeof(double) * nc,
-                                        cudaMemcpyHostToDevice, st));
-    }
     for (int64_t n = 0; n < nsteps && r == FVH_OK; ++n) {
       fvh::mixed::step_flags f = chunk_flags(n, nsteps);
-      if (mixed && n == 0) f.src = &hv;
+      if (n == 0) f.src = &hv;
       if (n + 1 == nsteps) f.out = &hv;
       r = solver_step_enqueue(s, dev_state, st, {}, f);
     }

@@ -70,7 +70,8 @@ template <int D>
 cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
                       const fvh_params &p, const double *soln_time, double *dt,
                       double *partial, int nblocks, fvh_device_status *status,
-                      cudaStream_t st, const double *slot_dx = nullptr);
+                      cudaStream_t st, const double *slot_dx = nullptr,
+                      const fvh_state_view *src = nullptr);
 template <int D>
 cudaError_t launch_gradients(const fvh_mesh_view &m, const fvh_state_view &s,
                              const fvh_gradient_view &g, const fvh_params &p,

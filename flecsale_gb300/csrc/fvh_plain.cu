@@ -271,13 +271,24 @@ __device__ __forceinline__ double cell_dt_inv(A &ar, const fvh_mesh_view &m,
   return dt_inv;
 }
 
+// With has_src the state is read from src (e.g. host-mapped planes of a caller
+// that holds its state in host memory) and stored into s as it goes, all but
+// the temperature, which no kernel of the step reads.
 template <int D, bool PRE>
 __global__ void __launch_bounds__(kDtThreads)
 dt_partial_kernel(const fvh_mesh_view m, const fvh_state_view s, double *partial,
-                  const double *__restrict__ slot_dx) {
+                  const double *__restrict__ slot_dx, const fvh_state_view src, int has_src) {
   double dt_inv = 0;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m.num_cells;
        c += gridDim.x * blockDim.x) {
+    if (has_src) {
+      s.density[c] = src.density[c];
+#pragma unroll
+      for (int i = 0; i < D; ++i) s.velocity[i][c] = src.velocity[i][c];
+      s.internal_energy[c] = src.internal_energy[c];
+      s.pressure[c] = src.pressure[c];
+      s.sound_speed[c] = src.sound_speed[c];
+    }
     arith_opt ar;
     double cell = cell_dt_inv<D, PRE>(ar, m, s, c, slot_dx);
     if (ar.rare) {
@@ -429,24 +440,38 @@ __device__ __forceinline__ void load_dx(const double *__restrict__ p, double *dx
   }
 }
 
+// Plane k of the reconstructed variables (d, v.., e, p, a) of a state and of
+// its gradients (component i).
 template <int D>
-__device__ __forceinline__ void load_values(const fvh_state_view &s, int c, double *u) {
-  int i = 0;
-  u[i++] = s.density[c];
-#pragma unroll
-  for (int d = 0; d < D; ++d) u[i++] = s.velocity[d][c];
-  u[i++] = s.internal_energy[c];
-  u[i++] = s.pressure[c];
-  u[i++] = s.sound_speed[c];
+__device__ __forceinline__ const double *state_plane(const fvh_state_view &s, int k) {
+  return k == 0 ? s.density
+                : k <= D ? s.velocity[k - 1]
+                         : k == D + 1 ? s.internal_energy
+                                      : k == D + 2 ? s.pressure : s.sound_speed;
+}
+template <int D>
+__device__ __forceinline__ double *grad_plane(const fvh_gradient_view &g, int k, int i) {
+  return k == 0 ? g.density[i]
+                : k <= D ? g.velocity[k - 1][i]
+                         : k == D + 1 ? g.internal_energy[i]
+                                      : k == D + 2 ? g.pressure[i] : g.sound_speed[i];
 }
 
-// The limited gradients gu of cell c0 (rows: the reconstructed variables d,
-// v.., e, p, a).
-template <int D, bool LIMIT, bool PRE, class A>
+template <int D, int K0, int NK>
+__device__ __forceinline__ void load_values(const fvh_state_view &s, int c, double *u) {
+#pragma unroll
+  for (int k = 0; k < NK; ++k) u[k] = state_plane<D>(s, K0 + k)[c];
+}
+
+// The limited gradients gu of cell c0 for the reconstructed variables
+// K0 .. K0+NK-1 (of d, v.., e, p, a).  Each variable's gradient and limiter
+// depend on that variable alone, so the variables can be taken in groups, each
+// in its own pass over the neighbours (fewer live registers, same results).
+template <int D, int K0, int NK, bool LIMIT, bool PRE, class A>
 __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
                                                const fvh_state_view &s, const tables &t,
-                                               int c0, double (&gu)[D + 4][D]) {
-  constexpr int NV = D + 4;
+                                               int c0, double (&gu)[NK][D]) {
+  constexpr int NV = NK;
   constexpr int W = lsq_width<D>::value;
   constexpr double tol = 1.e-9;
   double x0[D];
@@ -455,7 +480,7 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
     for (int i = 0; i < D; ++i) x0[i] = m.cell_centroid[i][c0];
   }
   double u0[NV];
-  load_values<D>(s, c0, u0);
+  load_values<D, K0, NK>(s, c0, u0);
   double dudx[NV][D];
 #pragma unroll
   for (int k = 0; k < NV; ++k)
@@ -465,7 +490,7 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
   for (int q = q0; q < q1; ++q) {
     const int c1 = m.cell_nbrs[q];
     double u1[NV];
-    load_values<D>(s, c1, u1);
+    load_values<D, K0, NK>(s, c1, u1);
     double dx[D];
     if (PRE) {
       load_dx<D>(t.nbr_dx + (size_t)q * D, dx);
@@ -564,23 +589,14 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
     // a variable some vertex value departs from by more than tol: they are
     // taken then, in a second pass over the neighbours (whose values are
     // still in cache), as order keys
-    const double *plane[NV];
-    {
-      int i = 0;
-      plane[i++] = s.density;
-#pragma unroll
-      for (int d = 0; d < D; ++d) plane[i++] = s.velocity[d];
-      plane[i++] = s.internal_energy;
-      plane[i++] = s.pressure;
-      plane[i++] = s.sound_speed;
-    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       long long kphi = okey(1.0);
       if (kpos[k] > ktol || kneg[k] < kntol) {
+        const double *plane = state_plane<D>(s, K0 + k);
         long long kmin = okey(u0[k]), kmax = kmin;
         for (int q = q0; q < q1; ++q) {
-          const long long k1 = okey(plane[k][m.cell_nbrs[q]]);
+          const long long k1 = okey(plane[m.cell_nbrs[q]]);
           kmin = (k1 < kmin) ? k1 : kmin;  // std::min(u1, umin)
           kmax = (kmax < k1) ? k1 : kmax;  // std::max(u1, umax)
         }
@@ -611,37 +627,47 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
   }
 }
 
-// 2D: 6 blocks of 128 per SM (at most 85 registers) measured faster than the
-// compiler's own choice (128 registers, 4 blocks); 3D spills at that bound
+// the gradients of variables K0 .. K0+NK-1 of cell c0, stored
+template <int D, int K0, int NK, bool LIMIT, bool PRE>
+__device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh_state_view &s,
+                                               const fvh_gradient_view &g, const tables &t,
+                                               int c0) {
+  double gu[NK][D];
+  arith_opt ar;
+  cell_gradients<D, K0, NK, LIMIT, PRE>(ar, m, s, t, c0, gu);
+  if (ar.rare) {
+    arith_hw hw;
+    cell_gradients<D, K0, NK, LIMIT, PRE>(hw, m, s, t, c0, gu);
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k)
+#pragma unroll
+    for (int i = 0; i < D; ++i) grad_plane<D>(g, K0 + k, i)[c0] = gu[k][i];
+}
+
+// Blocks of 128 per SM the kernels are compiled for.  2D: 6 (at most 85
+// registers) measured faster than the compiler's own choice (128 registers, 4
+// blocks).  3D (192^3 hex, ms per step): fluxes 4 blocks (128 registers, some
+// spills) 57.5 against 59.8 with 1 (240 registers); gradients 3 blocks (168)
+// 57.8 against 59.8 with 1 (218) and 58.7 with 4.
 template <int D>
-constexpr int min_blocks() { return D == 2 ? 6 : 1; }
+constexpr int min_blocks() { return D == 2 ? 6 : 4; }
+template <int D>
+constexpr int grad_min_blocks() { return D == 2 ? 6 : 3; }
+// variables per neighbour pass of the gradients: all of them in 2D; in 3D
+// (7 variables x 3 components) two passes, d v and e p a
+template <int D>
+__host__ __device__ constexpr int grad_split() { return D == 2 ? D + 4 : D + 1; }
 
 template <int D, bool LIMIT, bool PRE>
-__global__ void __launch_bounds__(kCellThreads, min_blocks<D>())
+__global__ void __launch_bounds__(kCellThreads, grad_min_blocks<D>())
 gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
                  const tables t) {
-  constexpr int NV = D + 4;
+  constexpr int NV = D + 4, S = grad_split<D>();
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (c0 >= m.num_cells) return;
-  double gu[NV][D];
-  {
-    arith_opt ar;
-    cell_gradients<D, LIMIT, PRE>(ar, m, s, t, c0, gu);
-    if (ar.rare) {
-      arith_hw hw;
-      cell_gradients<D, LIMIT, PRE>(hw, m, s, t, c0, gu);
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < D; ++i) {
-    int k = 0;
-    g.density[i][c0] = gu[k++][i];
-#pragma unroll
-    for (int d = 0; d < D; ++d) g.velocity[d][i][c0] = gu[k++][i];
-    g.internal_energy[i][c0] = gu[k++][i];
-    g.pressure[i][c0] = gu[k++][i];
-    g.sound_speed[i][c0] = gu[k++][i];
-  }
+  gradient_group<D, 0, S, LIMIT, PRE>(m, s, g, t, c0);
+  if constexpr (S < NV) gradient_group<D, S, NV - S, LIMIT, PRE>(m, s, g, t, c0);
 }
 
 // ---------------------------------------------------------------------------
@@ -906,11 +932,14 @@ template <int D>
 cudaError_t launch_dt(const fvh_mesh_view &m, const fvh_state_view &s,
                       const fvh_params &p, const double *soln_time, double *dt,
                       double *partial, int nblocks, fvh_device_status *status,
-                      cudaStream_t st, const double *slot_dx) {
+                      cudaStream_t st, const double *slot_dx, const fvh_state_view *src) {
+  const fvh_state_view from = src ? *src : s;
   if (slot_dx)
-    dt_partial_kernel<D, true><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, slot_dx);
+    dt_partial_kernel<D, true><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, slot_dx, from,
+                                                               src ? 1 : 0);
   else
-    dt_partial_kernel<D, false><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, nullptr);
+    dt_partial_kernel<D, false><<<nblocks, kDtThreads, 0, st>>>(m, s, partial, nullptr, from,
+                                                                src ? 1 : 0);
   dt_final_kernel<<<1, kDtThreads, 0, st>>>(partial, nblocks, p, soln_time, dt, status);
   return cudaGetLastError();
 }
@@ -1013,7 +1042,7 @@ cudaError_t launch_update(const fvh_mesh_view &m, const fvh_params &p, const dou
   template cudaError_t launch_dt<D>(const fvh_mesh_view &, const fvh_state_view &,     \
                                     const fvh_params &, const double *, double *,      \
                                     double *, int, fvh_device_status *, cudaStream_t,  \
-                                    const double *);                                   \
+                                    const double *, const fvh_state_view *);           \
   template cudaError_t launch_gradients<D>(const fvh_mesh_view &, const fvh_state_view &, \
                                            const fvh_gradient_view &, const fvh_params &, \
                                            cudaStream_t, const tables &);              \

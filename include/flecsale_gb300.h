@@ -488,12 +488,11 @@ fvh_status fvh_state_download(const fvh_state_view *src, int32_t dim,
  * in host memory: upload the
  * state, advance nsteps time steps, download it, then synchronise.  Solution
  * time in/out through *soln_time.  With pinned host planes (cudaHostAlloc /
- * cudaHostRegister) the last update writes the new state to host memory
- * directly, overlapping the download with the kernel; in the mixed form the
- * first pack also reads the state from host memory, and in the FP64 form only
- * the planes the step reads are copied up (all but the temperature, which the
- * step rewrites).  The results and the device state afterwards are the same
- * as with copies. */
+ * cudaHostRegister) the first kernel (the mixed form's pack, the FP64 form's
+ * dt) reads the state from host memory and the last update writes the new
+ * state to it directly, overlapping the transfers with the step; the
+ * temperature plane is not read (the step rewrites it).  The results and the
+ * device state afterwards are the same as with copies. */
 fvh_status fvh_solver_advance_host(fvh_solver *s, const fvh_state_view *dev_state,
                                    double *host_planes, int64_t nsteps,
                                    double *soln_time, fvh_stream_t stream);
