@@ -27,6 +27,14 @@
 // (arith_opt); if any operand was of a kind they do not handle (subnormal,
 // infinite, NaN, beyond 2^+-500) the unit is evaluated again with the FP64
 // instructions (arith_hw) and that result is kept.
+//
+// Code size: the integer forms inline to tens of instructions per product, so
+// a fully unrolled kernel outgrows the SM's instruction cache and its warps
+// stall on instruction fetch.  The kernels keep their neighbour and vertex
+// loops rolled, evaluate each physical flux once per side (selecting the
+// state instead of branching into copies), and take products, quotients and
+// the FP64 redo of a rare unit in out-of-line calls (2.27 -> 1.85 ms per 2D
+// step on the 1024^2 workload).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -38,12 +46,42 @@
 namespace fvh {
 namespace plain {
 
+// Products and quotients in out-of-line calls (a call costs a few
+// instructions; inlining them everywhere made the kernels too large for the
+// instruction cache).  An operand the integer path leaves to the hardware is
+// signalled by a NaN that path never returns (its results are zeros or normal
+// numbers).
+constexpr unsigned kRareHi = 0x7ff4deadu, kRareLo = 0x0badf00du;
+__device__ __noinline__ double mul_call(double a, double b) {
+  unsigned rare = 0;
+  const double q = sf64::mul_opt(a, b, rare);
+  return rare ? sf64::join(kRareLo, kRareHi) : q;
+}
+__device__ __noinline__ double div_call(double a, double b) {
+  unsigned rare = 0;
+  const double q = sf64::div_opt(a, b, rare);
+  return rare ? sf64::join(kRareLo, kRareHi) : q;
+}
+__device__ __forceinline__ bool signals_rare(double q) {
+  unsigned lo, hi;
+  sf64::halves(q, lo, hi);
+  return (hi == kRareHi) & (lo == kRareLo);
+}
+
 // Products and quotients of one unit of work: on the integer pipes, noting
 // any operand they leave to the hardware ...
 struct arith_opt {
   unsigned rare = 0;
-  __device__ __forceinline__ double mul(double a, double b) { return sf64::mul_opt(a, b, rare); }
-  __device__ __forceinline__ double quo(double a, double b) { return sf64::div_opt(a, b, rare); }
+  __device__ __forceinline__ double mul(double a, double b) {
+    const double q = mul_call(a, b);
+    rare |= (unsigned)signals_rare(q);
+    return q;
+  }
+  __device__ __forceinline__ double quo(double a, double b) {
+    const double q = div_call(a, b);
+    rare |= (unsigned)signals_rare(q);
+    return q;
+  }
 };
 // ... and with the FP64 instructions (the evaluation kept when `rare`)
 struct arith_hw {
@@ -157,22 +195,20 @@ __device__ __forceinline__ void hlle(A &ar, const prim<D> &l, const prim<D> &r,
   const double vnl = dot<D>(ar, l.v, n), vnr = dot<D>(ar, r.v, n);
   const double lambda_l = smin(vnl - l.a, vnr - r.a);
   const double lambda_r = smax(vnl + l.a, vnr + r.a);
-  if (ge0(lambda_l)) {
-    phys_flux<D>(ar, l, n, f);
-  } else if (le0(lambda_r)) {
-    phys_flux<D>(ar, r, n, f);
-  } else {
-    double fl[D + 2], fr[D + 2], du[D + 2];
-    phys_flux<D>(ar, l, n, fl);
-    phys_flux<D>(ar, r, n, fr);
-    const double c1 = ar.mul(lambda_l, lambda_r);
-    const double c2 = lambda_r - lambda_l;
-    const double c2inv = ar.quo(1, c2);
-    solution_delta<D>(ar, l, r, du);
+  // one physical-flux evaluation per side: the upwind side's (or the left
+  // side's when both are needed), then the right side's if both are
+  const bool up_l = ge0(lambda_l), up_r = !up_l && le0(lambda_r);
+  phys_flux<D>(ar, up_r ? r : l, n, f);
+  if (up_l || up_r) return;
+  double fr[D + 2], du[D + 2];
+  phys_flux<D>(ar, r, n, fr);
+  const double c1 = ar.mul(lambda_l, lambda_r);
+  const double c2 = lambda_r - lambda_l;
+  const double c2inv = ar.quo(1, c2);
+  solution_delta<D>(ar, l, r, du);
 #pragma unroll
-    for (int i = 0; i < D + 2; ++i)
-      f[i] = ar.mul(c2inv, ar.mul(lambda_r, fl[i]) - ar.mul(lambda_l, fr[i]) + ar.mul(c1, du[i]));
-  }
+  for (int i = 0; i < D + 2; ++i)
+    f[i] = ar.mul(c2inv, ar.mul(lambda_r, f[i]) - ar.mul(lambda_l, fr[i]) + ar.mul(c1, du[i]));
 }
 
 template <int D, class A>
@@ -197,33 +233,32 @@ __device__ __forceinline__ void hllc(A &ar, const prim<D> &l, const prim<D> &r,
   const double vnl = dot<D>(ar, l.v, n), vnr = dot<D>(ar, r.v, n);
   const double sL = smin(vnl - l.a, vnr - r.a);
   const double sR = smax(vnl + l.a, vnr + r.a);
-  if (ge0(sL)) {
-    phys_flux<D>(ar, l, n, f);
-    return;
+  // one physical-flux evaluation: of the upwind side, or of the star
+  // region's side, which then takes its correction
+  const bool up_l = ge0(sL), up_r = !up_l && le0(sR), star = !(up_l || up_r);
+  double ml = 0, mr = 0, sM = 0;
+  bool left = up_l;
+  if (star) {
+    ml = ar.mul(l.d, sL - vnl);
+    mr = ar.mul(r.d, sR - vnr);
+    sM = ar.quo(r.p - l.p + ar.mul(ml, vnl) - ar.mul(mr, vnr), ml - mr);
+    left = ge0(sM);
   }
-  if (le0(sR)) {
-    phys_flux<D>(ar, r, n, f);
-    return;
-  }
-  const double ml = ar.mul(l.d, sL - vnl);
-  const double mr = ar.mul(r.d, sR - vnr);
-  const double sM = ar.quo(r.p - l.p + ar.mul(ml, vnl) - ar.mul(mr, vnr), ml - mr);
-  const bool left = ge0(sM);
   const prim<D> &u = left ? l : r;
+  phys_flux<D>(ar, u, n, f);
+  if (!star) return;
   const double sK = left ? sL : sR;
   const double mK = left ? ml : mr;
   const double vnK = left ? vnl : vnr;
-  double fk[D + 2];
-  phys_flux<D>(ar, u, n, fk);
   const double EK = ar.mul(u.d, total_energy<D>(ar, u));
   const double fac = ar.quo(mK, sK - sM);
   const double dvn = sM - vnK;
-  f[0] = fk[0] + ar.mul(sK, fac - u.d);
+  f[0] = f[0] + ar.mul(sK, fac - u.d);
 #pragma unroll
   for (int i = 0; i < D; ++i)
-    f[1 + i] = fk[1 + i] +
+    f[1 + i] = f[1 + i] +
                ar.mul(sK, ar.mul(fac, u.v[i] + ar.mul(dvn, n[i])) - ar.mul(u.d, u.v[i]));
-  f[D + 1] = fk[D + 1] +
+  f[D + 1] = f[D + 1] +
              ar.mul(sK, ar.mul(fac, ar.quo(EK, u.d) + ar.mul(dvn, sM + ar.quo(u.p, mK))) - EK);
 }
 
@@ -487,6 +522,7 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
 #pragma unroll
     for (int j = 0; j < D; ++j) dudx[k][j] = 0;
   const int q0 = m.cell_nbr_offsets[c0], q1 = m.cell_nbr_offsets[c0 + 1];
+  #pragma unroll 1
   for (int q = q0; q < q1; ++q) {
     const int c1 = m.cell_nbrs[q];
     double u1[NV];
@@ -565,6 +601,7 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
       for (int i = 0; i < D; ++i) graded[k] = graded[k] || !is_zero(gu[k][i]);
     }
     const int r0 = m.cell_vertex_offsets[c0], r1 = m.cell_vertex_offsets[c0 + 1];
+    #pragma unroll 1
     for (int rr = r0; rr < r1; ++rr) {
       double dxv[D];
       if (PRE) {
@@ -595,6 +632,7 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
       if (kpos[k] > ktol || kneg[k] < kntol) {
         const double *plane = state_plane<D>(s, K0 + k);
         long long kmin = okey(u0[k]), kmax = kmin;
+        #pragma unroll 1
         for (int q = q0; q < q1; ++q) {
           const long long k1 = okey(plane[m.cell_nbrs[q]]);
           kmin = (k1 < kmin) ? k1 : kmin;  // std::min(u1, umin)
@@ -628,6 +666,27 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
 }
 
 // the gradients of variables K0 .. K0+NK-1 of cell c0, stored
+template <int D, int K0, int NK, bool LIMIT, bool PRE, class A>
+__device__ __forceinline__ void gradient_group_with(A &ar, const fvh_mesh_view &m,
+                                                    const fvh_state_view &s,
+                                                    const fvh_gradient_view &g, const tables &t,
+                                                    int c0) {
+  double gu[NK][D];
+  cell_gradients<D, K0, NK, LIMIT, PRE>(ar, m, s, t, c0, gu);
+#pragma unroll
+  for (int k = 0; k < NK; ++k)
+#pragma unroll
+    for (int i = 0; i < D; ++i) grad_plane<D>(g, K0 + k, i)[c0] = gu[k][i];
+}
+
+template <int D, int K0, int NK, bool LIMIT, bool PRE>
+__device__ __noinline__ void gradient_group_hw(const fvh_mesh_view &m, const fvh_state_view &s,
+                                               const fvh_gradient_view &g, const tables &t,
+                                               int c0) {
+  arith_hw hw;
+  gradient_group_with<D, K0, NK, LIMIT, PRE>(hw, m, s, g, t, c0);
+}
+
 template <int D, int K0, int NK, bool LIMIT, bool PRE>
 __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh_state_view &s,
                                                const fvh_gradient_view &g, const tables &t,
@@ -636,8 +695,8 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
   arith_opt ar;
   cell_gradients<D, K0, NK, LIMIT, PRE>(ar, m, s, t, c0, gu);
   if (ar.rare) {
-    arith_hw hw;
-    cell_gradients<D, K0, NK, LIMIT, PRE>(hw, m, s, t, c0, gu);
+    gradient_group_hw<D, K0, NK, LIMIT, PRE>(m, s, g, t, c0);
+    return;
   }
 #pragma unroll
   for (int k = 0; k < NK; ++k)
@@ -645,15 +704,17 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
     for (int i = 0; i < D; ++i) grad_plane<D>(g, K0 + k, i)[c0] = gu[k][i];
 }
 
-// Blocks of 128 per SM the kernels are compiled for.  2D: 6 (at most 85
-// registers) measured faster than the compiler's own choice (128 registers, 4
-// blocks).  3D (192^3 hex, ms per step): fluxes 4 blocks (128 registers, some
-// spills) 57.5 against 59.8 with 1 (240 registers); gradients 3 blocks (168)
-// 57.8 against 59.8 with 1 (218) and 58.7 with 4.
+// Blocks of 128 per SM the kernels are compiled for.  2D (1024^2 workload, ms
+// per step): gradients 7 (at most 73 registers) 1.813 against 1.845 with 6
+// and 1.887 with 5; fluxes 6 (80 registers) 1.845 against 1.870 with 5 and
+// 1.845 with 7.  3D (192^3 hex): fluxes 4 blocks (128 registers, some spills)
+// 57.5 against 59.8 with 1 (240 registers); gradients 3 blocks (168) 57.8
+// against 59.8 with 1 (218) and 58.7 with 4 (measured before the products
+// moved out of line).
 template <int D>
 constexpr int min_blocks() { return D == 2 ? 6 : 4; }
 template <int D>
-constexpr int grad_min_blocks() { return D == 2 ? 6 : 3; }
+constexpr int grad_min_blocks() { return D == 2 ? 7 : 3; }
 // variables per neighbour pass of the gradients: all of them in 2D; in 3D
 // (7 variables x 3 components) two passes, d v and e p a
 template <int D>
@@ -771,6 +832,20 @@ __device__ __forceinline__ void face_flux(A &ar, const fvh_mesh_view &m,
 }
 
 template <int D, int KIND, bool SECOND, bool PRE>
+__device__ __noinline__ void face_flux_hw(const fvh_mesh_view &m, const fvh_state_view &s,
+                                          const fvh_gradient_view &g, const fvh_flux_view &fl,
+                                          int f, int2 cc, int swap, int outflow,
+                                          const double *face_dx) {
+  double F[D + 2];
+  arith_hw hw;
+  face_flux<D, KIND, SECOND, PRE>(hw, m, s, g, f, cc, swap != 0, outflow != 0, face_dx, F);
+  fl.mass[f] = F[0];
+#pragma unroll
+  for (int i = 0; i < D; ++i) fl.momentum[i][f] = F[1 + i];
+  fl.energy[f] = F[D + 1];
+}
+
+template <int D, int KIND, bool SECOND, bool PRE>
 __global__ void __launch_bounds__(kFaceThreads, min_blocks<D>())
 fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
               const fvh_flux_view fl, int swap, int outflow, const double *__restrict__ face_dx) {
@@ -782,8 +857,8 @@ fluxes_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_
     arith_opt ar;
     face_flux<D, KIND, SECOND, PRE>(ar, m, s, g, f, cc, swap != 0, outflow != 0, face_dx, F);
     if (ar.rare) {
-      arith_hw hw;
-      face_flux<D, KIND, SECOND, PRE>(hw, m, s, g, f, cc, swap != 0, outflow != 0, face_dx, F);
+      face_flux_hw<D, KIND, SECOND, PRE>(m, s, g, fl, f, cc, swap, outflow, face_dx);
+      return;
     }
   }
   fl.mass[f] = F[0];
