@@ -617,8 +617,25 @@ def run_ours(args):
                                "share": v[0] * v[1] / profiled_step,
                                "achieved_gbs": ab[k] / (v[0] * scale * 1e-3) / 1e9,
                                "frac": ab[k] / (v[0] * scale * 1e-3) / 1e9 / hbm,
-                               "fp64_pipe_active": pipes.get(f"{form}:{k}", {}).get("fp64")}
+                               "fp64_pipe_active": pipes.get(f"{form}:{k}", {}).get("fp64"),
+                               "alu_pipe_active": pipes.get(f"{form}:{k}", {}).get("alu"),
+                               "dram_traffic": traffic.get(f"{form}:{k}", {}).get("bytes")}
                            for k, v in p.items()}}
+        if form == "mixed" and dom in ("gradients", "pack_dt"):
+            # The per-task bytes of the reference dataflow (FP64 values, int32
+            # connectivity), the same per-cell figure as the plain form's, for
+            # comparability between forms; the kernel's own minimum (FP32
+            # records) beside it.
+            task = {"gradients": "gradients", "pack_dt": "dt"}[dom]
+            sb = algorithmic_bytes(mesh, "fp64")[task]
+            out.update({"algorithmic_bytes_per_launch": sb,
+                        "achieved": sb / (dur * 1e-3) / 1e9,
+                        "frac": sb / (dur * 1e-3) / 1e9 / hbm,
+                        "bytes_basis": f"reference-dataflow bytes of the {task} task "
+                                       f"({sb / mesh.num_cells:.0f} B/cell, as for the plain form)",
+                        "kernel_bytes_per_launch": ab[dom],
+                        "achieved_kernel_bytes": achieved,
+                        "frac_kernel_bytes": achieved / hbm})
         return out
 
     zu = lambda ms: ws * nc * args.steps / (ms * 1e-3)
@@ -638,9 +655,10 @@ def run_ours(args):
 
     fp64_roof = roofline("fp64")
     fp64_roof["pipe_bound"] = "fp64"
-    fp64_roof["note"] = ("the FP64 kernels are bound by GB300's FP64 pipe (2 FP64 operations "
-                         "per clock per SM); fp64_pipe_active per kernel is the ncu figure "
-                         "(profiles/pipe_utilization.json)")
+    fp64_roof["note"] = ("the bit-exact FP64 kernels are bound by GB300's FP64 pipe (2 FP64 "
+                         "operations per clock per SM) and by the integer pipe that computes "
+                         "their products and quotients; fp64_pipe_active / alu_pipe_active per "
+                         "kernel are the ncu figures (profiles/pipe_utilization.json)")
     line = {
         "metric": METRIC,
         "value": zu(results["fp64"]["ms"]),

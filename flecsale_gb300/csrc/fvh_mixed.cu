@@ -73,12 +73,16 @@ struct stage_run {
 
 struct stage_tables {
   int nchunks = 0;
+  // layout of one stage buffer (bytes), sized for this mesh's largest chunk:
+  // pack records (32 B) at 0, centroids (16 B) at cen_at, vertex coordinates
+  // (16 B) at vtx_at, the chunk's topology block at topo_at
+  int cen_at = 0, vtx_at = 0, topo_at = 0, stage_bytes = 0;
   const int *cells = nullptr;                // [nchunks * kStageCells] cell ids, -1 = none
   const int *run_off = nullptr;              // [nchunks + 1] into runs
   const stage_run *runs = nullptr;
   const long long *topo_off = nullptr;       // [nchunks + 1] byte offsets into topo
   const unsigned *bytes = nullptr;           // [nchunks] bytes staged per chunk
-  const unsigned short *topo = nullptr;      // per chunk: see setup_stage_host
+  const unsigned *topo = nullptr;            // per chunk: see setup_stage_host
 };
 
 struct workspace {
@@ -966,20 +970,17 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 // and their vertex neighbours) and the coordinates of its cells' vertices; on
 // a mesh numbered row by row these sets are a few runs of consecutive ids.  The
 // setup lists each chunk's runs and packs, per cell, its own record's position
-// and those of its neighbours and vertices in the chunk's staged set (16 bits
-// each).  A persistent kernel posts the copies of chunk i+1 (one bulk copy per
+// and those of its neighbours and vertices in the chunk's staged set (a byte
+// each, four to a 32-bit word).  A persistent kernel posts the copies of chunk
+// i+1 (one bulk copy per
 // run and array, plus one for the chunk's topology; completion counted on an
 // mbarrier) while its threads compute chunk i from shared memory with the
 // arithmetic of gradients_kernel (cell_gradients_pairs), so both kernels give
 // the same bits.
-constexpr int kStageCells = 128;     // cells per chunk = threads per block
-constexpr int kStageMaxCells = 256;  // staged cell records per chunk
-constexpr int kStageMaxVerts = 192;  // staged vertex records per chunk
-constexpr int kStageTopoBytes = 2816;
-constexpr int kStagePackBytes = kStageMaxCells * 32;
-constexpr int kStageCenBytes = kStageMaxCells * 16;
-constexpr int kStageVtxBytes = kStageMaxVerts * 16;
-constexpr int kStageBytes = kStagePackBytes + kStageCenBytes + kStageVtxBytes + kStageTopoBytes;
+constexpr int kStageCells = 128;      // cells per chunk = threads per block
+constexpr int kStageMaxCells = 256;   // staged cell records per chunk (byte slots)
+constexpr int kStageMaxVerts = 256;   // staged vertex records per chunk
+constexpr int kStageMaxBytes = 24576; // one stage buffer at most (two per block)
 constexpr int kStageWaitPolls = 1 << 22;  // bounded waits on a chunk's copies
 
 template <bool LIMIT>
@@ -995,14 +996,14 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
     const int r0 = t.run_off[k], nr = t.run_off[k + 1] - r0;
     const long long tb0 = t.topo_off[k];
     const unsigned topo_bytes = (unsigned)(t.topo_off[k + 1] - tb0);
-    unsigned char *base = smem + (size_t)b * kStageBytes;
+    unsigned char *base = smem + (size_t)b * t.stage_bytes;
     // this buffer's earlier reads (ordered by the block barrier) come before
     // the copies that overwrite it
     tma::fence_proxy_async_shared();
     if (tid == 0) {
       tma::mbar_arrive_expect_tx(&bar[b], t.bytes[k]);
-      tma::bulk_g2s(base + kStagePackBytes + kStageCenBytes + kStageVtxBytes,
-                    reinterpret_cast<const unsigned char *>(t.topo) + tb0, topo_bytes, &bar[b]);
+      tma::bulk_g2s(base + t.topo_at, reinterpret_cast<const unsigned char *>(t.topo) + tb0,
+                    topo_bytes, &bar[b]);
     }
     __syncwarp();
     for (int r = tid; r < nr; r += 32) {
@@ -1010,11 +1011,11 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
       if (run.kind == 0) {
         tma::bulk_g2s(base + (size_t)run.slot * 32, pk + 2 * (size_t)run.first,
                       (unsigned)run.count * 32u, &bar[b]);
-        tma::bulk_g2s(base + kStagePackBytes + (size_t)run.slot * 16, w.ccen + run.first,
+        tma::bulk_g2s(base + t.cen_at + (size_t)run.slot * 16, w.ccen + run.first,
                       (unsigned)run.count * 16u, &bar[b]);
       } else {
-        tma::bulk_g2s(base + kStagePackBytes + kStageCenBytes + (size_t)run.slot * 16,
-                      w.vcoord + run.first, (unsigned)run.count * 16u, &bar[b]);
+        tma::bulk_g2s(base + t.vtx_at + (size_t)run.slot * 16, w.vcoord + run.first,
+                      (unsigned)run.count * 16u, &bar[b]);
       }
     }
   };
@@ -1044,23 +1045,26 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
     const int c0 = t.cells[(size_t)k * kStageCells + tid];
     const bool landed = tma::mbar_wait_bounded(&bar[b], (unsigned)(used[b] & 1), kStageWaitPolls);
     ++used[b];
-    const unsigned char *base = smem + (size_t)b * kStageBytes;
+    const unsigned char *base = smem + (size_t)b * t.stage_bytes;
     const float4 *spk = reinterpret_cast<const float4 *>(base);
-    const float4 *scen = reinterpret_cast<const float4 *>(base + kStagePackBytes);
-    const float4 *svtx = reinterpret_cast<const float4 *>(base + kStagePackBytes + kStageCenBytes);
-    const unsigned short *topo = reinterpret_cast<const unsigned short *>(
-        base + kStagePackBytes + kStageCenBytes + kStageVtxBytes);
+    const float4 *scen = reinterpret_cast<const float4 *>(base + t.cen_at);
+    const float4 *svtx = reinterpret_cast<const float4 *>(base + t.vtx_at);
+    const unsigned *topo = reinterpret_cast<const unsigned *>(base + t.topo_at);
     if (landed && c0 >= 0) {
-      const unsigned char *rec = reinterpret_cast<const unsigned char *>(topo) + topo[tid];
-      const int own = rec[0], nn = rec[1], nr = rec[2];
-      const unsigned char *nslot = rec + 3, *vslot = rec + 3 + nn;
+      // the cell's record: word 0 = own slot | nn << 8 | nr << 16, then the
+      // neighbour slots and the vertex slots, four bytes to a word each
+      const unsigned *rec = topo + (reinterpret_cast<const unsigned short *>(topo)[tid]);
+      const unsigned head = rec[0];
+      const int own = head & 0xffu, nn = (head >> 8) & 0xffu, nr = (head >> 16) & 0xffu;
+      const unsigned *nslot = rec + 1, *vslot = rec + 1 + ((nn + 3) >> 2);
+      auto byte_at = [](const unsigned *wd, int i) { return (int)((wd[i >> 2] >> ((i & 3) * 8)) & 0xffu); };
       const float4 a0 = spk[2 * own], b0 = spk[2 * own + 1];
       const float4 x0 = scen[own];
       const float xh[3] = {x0.x, x0.y, 0.f}, xl[3] = {x0.z, x0.w, 0.f};
       cell_gradients_pairs<2, LIMIT, 4>(
           w, c0, a0, b0, xh, xl, nn,
           [&](int q, float4 &a, float4 &bb, float *yh, float *yl) {
-            const int sl = nslot[q];
+            const int sl = byte_at(nslot, q);
             a = spk[2 * sl];
             bb = spk[2 * sl + 1];
             const float4 y = scen[sl];
@@ -1068,7 +1072,7 @@ gradients_staged_kernel(const fvh_mesh_view m, workspace w, const float4 *__rest
           },
           nr,
           [&](int r, float *vh, float *vl) {
-            const float4 v = svtx[vslot[r]];
+            const float4 v = svtx[byte_at(vslot, r)];
             vh[0] = v.x; vh[1] = v.y; vl[0] = v.z; vl[1] = v.w;
           });
     }
@@ -1717,12 +1721,13 @@ int colours(const workspace *w) { return w ? w->ncolours : 0; }
 // Tables of the staged 2D gradients (see gradients_staged_kernel), built on
 // the host from the mesh.  Chunks: kStageCells consecutive cells of the Morton
 // order of the centroids (16-bit quantised coordinates, bits interleaved).
-// Per chunk, a topology block: 16-bit word i (i < kStageCells) is the byte
-// offset of cell i's record (or 0xffff), a record is bytes (own slot, number
-// of neighbours nn, number of vertices nr, nn neighbour slots, nr vertex
-// slots) -- a chunk stages at most 256 cell and vertex records, so a slot
-// fits in a byte; the block is padded to 16 bytes.  A mesh with a chunk whose staged set or
-// topology does not fit keeps the global-memory kernel (nchunks stays 0).
+// Per chunk, a topology block of 32-bit words: 16-bit entry i of the first
+// kStageCells / 2 words is the word offset of cell i's record (or 0xffff); a
+// record is a word (own slot | nn << 8 | nr << 16), then the nn neighbour
+// slots and the nr vertex slots, a byte each and four to a word -- a chunk
+// stages at most 256 cell and 256 vertex records, so a slot fits in a byte.
+// The stage buffers are sized for the mesh's largest chunk; a mesh with a
+// chunk that does not fit keeps the global-memory kernel (nchunks stays 0).
 static unsigned spread_bits16(unsigned x) {
   x &= 0xffffu;
   x = (x | (x << 8)) & 0x00ff00ffu;
@@ -1767,9 +1772,10 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
   std::sort(order.begin(), order.end());
   const int nchunks = (nc + kStageCells - 1) / kStageCells;
   std::vector<std::vector<stage_run>> runs(nchunks);
-  std::vector<std::vector<unsigned short>> topo(nchunks);
-  int fits = 1;
-#pragma omp parallel for schedule(dynamic, 16) reduction(& : fits)
+  std::vector<std::vector<unsigned>> topo(nchunks);
+  int fits = 1, max_cells = 0, max_verts = 0, max_topo = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(& : fits) \
+    reduction(max : max_cells, max_verts, max_topo)
   for (int k = 0; k < nchunks; ++k) {
     const int i0 = k * kStageCells, i1 = std::min(nc, i0 + kStageCells);
     std::vector<int> ids, vids;
@@ -1798,33 +1804,47 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
     add_runs(ids, 0);
     add_runs(vids, 1);
     auto pos = [](const std::vector<int> &v, int x) {
-      return (unsigned short)(std::lower_bound(v.begin(), v.end(), x) - v.begin());
+      return (unsigned)(std::lower_bound(v.begin(), v.end(), x) - v.begin());
     };
-    std::vector<unsigned char> bytes;
-    std::vector<unsigned short> index(kStageCells, 0xffffu);
+    constexpr int kIndexWords = kStageCells / 2;
+    std::vector<unsigned> words(kIndexWords, 0xffffffffu);
     bool ok = true;
     for (int i = i0; i < i1 && ok; ++i) {
       const int c = order[i].second;
       const int nn = nb_off[c + 1] - nb_off[c], nr = cv_off[c + 1] - cv_off[c];
-      ok = nn < 256 && nr < 256;
-      index[i - i0] = (unsigned short)(2 * kStageCells + bytes.size());
-      bytes.push_back((unsigned char)pos(ids, c));
-      bytes.push_back((unsigned char)nn);
-      bytes.push_back((unsigned char)nr);
-      for (int q = nb_off[c]; q < nb_off[c + 1]; ++q) bytes.push_back((unsigned char)pos(ids, nb[q]));
-      for (int r = cv_off[c]; r < cv_off[c + 1]; ++r) bytes.push_back((unsigned char)pos(vids, cv[r]));
+      ok = nn < 256 && nr < 256 && words.size() < 0xffffu;
+      const unsigned at = (unsigned)words.size();
+      unsigned &slot = words[(i - i0) / 2];
+      slot = (i - i0) % 2 == 0 ? ((slot & 0xffff0000u) | at) : ((slot & 0xffffu) | (at << 16));
+      words.push_back((unsigned)pos(ids, c) | ((unsigned)nn << 8) | ((unsigned)nr << 16));
+      auto put_bytes = [&](const int *v, int n, const std::vector<int> &set) {
+        for (int j = 0; j < n; j += 4) {
+          unsigned wd = 0;
+          for (int b = 0; b < 4 && j + b < n; ++b) wd |= (unsigned)pos(set, v[j + b]) << (8 * b);
+          words.push_back(wd);
+        }
+      };
+      put_bytes(nb.data() + nb_off[c], nn, ids);
+      put_bytes(cv.data() + cv_off[c], nr, vids);
     }
-    while (bytes.size() % 16) bytes.push_back(0);  // 16-byte multiple
-    if (!ok || 2 * kStageCells + bytes.size() > (size_t)kStageTopoBytes) {
+    while (words.size() % 4) words.push_back(0);  // 16-byte multiple
+    if (!ok) {
       fits = 0;
       continue;
     }
-    std::vector<unsigned short> &tb = topo[k];
-    tb = index;
-    for (size_t j = 0; j < bytes.size(); j += 2)
-      tb.push_back((unsigned short)(bytes[j] | (bytes[j + 1] << 8)));
+    max_cells = std::max(max_cells, (int)ids.size());
+    max_verts = std::max(max_verts, (int)vids.size());
+    max_topo = std::max(max_topo, (int)(4 * words.size()));
+    topo[k] = std::move(words);
   }
   if (!fits) return cudaSuccess;  // the global-memory kernel serves this mesh
+  auto up128 = [](int b) { return (b + 127) / 128 * 128; };
+  stage_tables t;
+  t.cen_at = up128(32 * max_cells);
+  t.vtx_at = t.cen_at + up128(16 * max_cells);
+  t.topo_at = t.vtx_at + up128(16 * max_verts);
+  t.stage_bytes = t.topo_at + up128(max_topo);
+  if (t.stage_bytes > kStageMaxBytes) return cudaSuccess;
   std::vector<int> cells((size_t)nchunks * kStageCells, -1);
   for (int i = 0; i < nc; ++i) cells[i] = order[i].second;
   std::vector<int> run_off(nchunks + 1, 0);
@@ -1832,21 +1852,21 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
   std::vector<unsigned> chunk_bytes(nchunks, 0);
   for (int k = 0; k < nchunks; ++k) {
     run_off[k + 1] = run_off[k] + (int)runs[k].size();
-    topo_off[k + 1] = topo_off[k] + 2 * (long long)topo[k].size();
-    chunk_bytes[k] = 2 * (unsigned)topo[k].size();
+    topo_off[k + 1] = topo_off[k] + 4 * (long long)topo[k].size();
+    chunk_bytes[k] = 4 * (unsigned)topo[k].size();
     for (const stage_run &r : runs[k]) chunk_bytes[k] += (unsigned)r.count * (r.kind == 0 ? 48u : 16u);
   }
   std::vector<stage_run> all(run_off[nchunks]);
-  std::vector<unsigned short> blob(topo_off[nchunks] / 2);
+  std::vector<unsigned> blob(topo_off[nchunks] / 4);
   for (int k = 0; k < nchunks; ++k) {
     std::copy(runs[k].begin(), runs[k].end(), all.begin() + run_off[k]);
-    std::copy(topo[k].begin(), topo[k].end(), blob.begin() + topo_off[k] / 2);
+    std::copy(topo[k].begin(), topo[k].end(), blob.begin() + topo_off[k] / 4);
   }
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t b_cells = up(sizeof(int) * cells.size()), b_off = up(sizeof(int) * run_off.size()),
                b_runs = up(sizeof(stage_run) * all.size()),
                b_toff = up(sizeof(long long) * topo_off.size()),
-               b_topo = up(sizeof(unsigned short) * blob.size()),
+               b_topo = up(sizeof(unsigned) * blob.size()),
                b_bytes = up(sizeof(unsigned) * chunk_bytes.size());
   char *base = nullptr;
   e = cudaMalloc(&base, b_cells + b_off + b_runs + b_toff + b_topo + b_bytes);
@@ -1859,20 +1879,18 @@ static cudaError_t setup_stage_host(workspace *w, const fvh_mesh_view &m) {
     p += span;
     return d;
   };
-  stage_tables t;
   t.nchunks = nchunks;
   t.cells = reinterpret_cast<const int *>(put(cells.data(), sizeof(int) * cells.size(), b_cells));
   t.run_off = reinterpret_cast<const int *>(put(run_off.data(), sizeof(int) * run_off.size(), b_off));
   t.runs = reinterpret_cast<const stage_run *>(put(all.data(), sizeof(stage_run) * all.size(), b_runs));
   t.topo_off = reinterpret_cast<const long long *>(
       put(topo_off.data(), sizeof(long long) * topo_off.size(), b_toff));
-  t.topo = reinterpret_cast<const unsigned short *>(
-      put(blob.data(), sizeof(unsigned short) * blob.size(), b_topo));
+  t.topo = reinterpret_cast<const unsigned *>(put(blob.data(), sizeof(unsigned) * blob.size(), b_topo));
   t.bytes = reinterpret_cast<const unsigned *>(
       put(chunk_bytes.data(), sizeof(unsigned) * chunk_bytes.size(), b_bytes));
   if (e != cudaSuccess) return e;
   // persistent grid: the blocks that fit on the device at once
-  const int smem = 2 * kStageBytes;
+  const int smem = 2 * t.stage_bytes;
   e = cudaFuncSetAttribute(gradients_staged_kernel<true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess)
@@ -1946,7 +1964,7 @@ static void launch_stage_bs(workspace *w, const fvh_mesh_view &m, const fvh_para
   if (SECOND) {
     dir ^= 1;
     if (D == 2 && staged && w->stage.nchunks > 0 && !pm.cell_problem) {
-      const int smem = 2 * kStageBytes;
+      const int smem = 2 * w->stage.stage_bytes;
       if (p.limiter == FVH_LIMITER_NONE)
         gradients_staged_kernel<false><<<w->stage_blocks, kStageCells, smem, st>>>(
             m, *w, pk_in, w->stage, dir, pm.status);

@@ -33,7 +33,7 @@
 // stall on instruction fetch.  The kernels keep their neighbour and vertex
 // loops rolled, evaluate each physical flux once per side (selecting the
 // state instead of branching into copies), and take products, quotients and
-// the FP64 redo of a rare unit in out-of-line calls (2.27 -> 1.85 ms per 2D
+// the FP64 redo of a rare unit in out-of-line calls (2.27 -> 1.77 ms per 2D
 // step on the 1024^2 workload).
 #include <cuda_runtime.h>
 
@@ -43,29 +43,29 @@
 #include "fvh_kernels.h"
 #include "fvh_sf64.cuh"
 
+
 namespace fvh {
 namespace plain {
 
 // Products and quotients in out-of-line calls (a call costs a few
 // instructions; inlining them everywhere made the kernels too large for the
-// instruction cache).  An operand the integer path leaves to the hardware is
-// signalled by a NaN that path never returns (its results are zeros or normal
-// numbers).
-constexpr unsigned kRareHi = 0x7ff4deadu, kRareLo = 0x0badf00du;
-__device__ __noinline__ double mul_call(double a, double b) {
-  unsigned rare = 0;
-  const double q = sf64::mul_opt(a, b, rare);
-  return rare ? sf64::join(kRareLo, kRareHi) : q;
+// instruction cache).  Each returns its result with the flag that an operand
+// was left to the hardware.
+struct flagged {
+  double q;
+  unsigned rare;
+};
+__device__ __noinline__ flagged mul_call(double a, double b) {
+  flagged r;
+  r.rare = 0;
+  r.q = sf64::mul_opt(a, b, r.rare);
+  return r;
 }
-__device__ __noinline__ double div_call(double a, double b) {
-  unsigned rare = 0;
-  const double q = sf64::div_opt(a, b, rare);
-  return rare ? sf64::join(kRareLo, kRareHi) : q;
-}
-__device__ __forceinline__ bool signals_rare(double q) {
-  unsigned lo, hi;
-  sf64::halves(q, lo, hi);
-  return (hi == kRareHi) & (lo == kRareLo);
+__device__ __noinline__ flagged div_call(double a, double b) {
+  flagged r;
+  r.rare = 0;
+  r.q = sf64::div_opt(a, b, r.rare);
+  return r;
 }
 
 // Products and quotients of one unit of work: on the integer pipes, noting
@@ -73,14 +73,14 @@ __device__ __forceinline__ bool signals_rare(double q) {
 struct arith_opt {
   unsigned rare = 0;
   __device__ __forceinline__ double mul(double a, double b) {
-    const double q = mul_call(a, b);
-    rare |= (unsigned)signals_rare(q);
-    return q;
+    const flagged r = mul_call(a, b);
+    rare |= r.rare;
+    return r.q;
   }
   __device__ __forceinline__ double quo(double a, double b) {
-    const double q = div_call(a, b);
-    rare |= (unsigned)signals_rare(q);
-    return q;
+    const flagged r = div_call(a, b);
+    rare |= r.rare;
+    return r.q;
   }
 };
 // ... and with the FP64 instructions (the evaluation kept when `rare`)
@@ -707,14 +707,12 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
 // Blocks of 128 per SM the kernels are compiled for.  2D (1024^2 workload, ms
 // per step): gradients 7 (at most 73 registers) 1.813 against 1.845 with 6
 // and 1.887 with 5; fluxes 6 (80 registers) 1.845 against 1.870 with 5 and
-// 1.845 with 7.  3D (192^3 hex): fluxes 4 blocks (128 registers, some spills)
-// 57.5 against 59.8 with 1 (240 registers); gradients 3 blocks (168) 57.8
-// against 59.8 with 1 (218) and 58.7 with 4 (measured before the products
-// moved out of line).
+// 1.845 with 7.  3D (96^3 hex, ms per step): gradients and fluxes 5 blocks
+// (96 registers) 5.68 against 5.92 with 3 and 4 and 5.88 with 4 and 5.
 template <int D>
-constexpr int min_blocks() { return D == 2 ? 6 : 4; }
+constexpr int min_blocks() { return D == 2 ? 6 : 5; }
 template <int D>
-constexpr int grad_min_blocks() { return D == 2 ? 7 : 3; }
+constexpr int grad_min_blocks() { return D == 2 ? 7 : 5; }
 // variables per neighbour pass of the gradients: all of them in 2D; in 3D
 // (7 variables x 3 components) two passes, d v and e p a
 template <int D>
