@@ -595,6 +595,10 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
   constexpr float tol = 1.e-9f;
   float M[6] = {0, 0, 0, 0, 0, 0};
   float b[NV][D];
+  // neighbour extrema (tasks.h:232-236), taken in the same pass
+  float umin[NV], umax[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
 #pragma unroll
   for (int k = 0; k < NV; ++k)
 #pragma unroll
@@ -622,6 +626,8 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
       const float du = u1[k] - u0[k];
 #pragma unroll
       for (int j = 0; j < D; ++j) b[k][j] += du * dx[j];
+      umin[k] = fminf(u1[k], umin[k]);
+      umax[k] = fmaxf(u1[k], umax[k]);
     }
   }
   float g[NV][D];
@@ -671,27 +677,6 @@ __device__ __forceinline__ void cell_gradients(const fvh_mesh_view &m, const wor
 #pragma unroll
       for (int i = 0; i < D; ++i) dxv[i] = __fadd_rn(__fsub_rn(vh[i], xh[i]), __fsub_rn(vl[i], xl[i]));
       vertex(dxv);
-    }
-    // the neighbour extrema (tasks.h:232-236) only when some variable can be
-    // limited: a second pass over the neighbours (min / max do not depend on
-    // the order, so the values are those of a single pass)
-    float umin[NV], umax[NV];
-    bool need = false;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      umin[k] = umax[k] = u0[k];
-      need = need || dpos[k] > tol || dneg[k] < -tol;
-    }
-    if (need) {
-      for (int q = 0; q < nn; ++q) {
-        float u1[NV], yh[3], yl[3];
-        nbr(q, u1, yh, yl);
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-          umin[k] = fminf(u1[k], umin[k]);
-          umax[k] = fmaxf(u1[k], umax[k]);
-        }
-      }
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
@@ -753,6 +738,13 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
   float m11 = 0.f, m22 = 0.f;
   float2 bs[NP][D];  // sum (u_q - u0) dx_q for slot pairs
   float bo[D];       // and for the odd slot
+  // neighbour extrema (tasks.h:232-236), taken in the same pass
+  float umin[NV], umax[NV];
+  {
+    const float u0[8] = {a0.x, a0.y, a0.z, a0.w, b0.x, b0.y, b0.z, b0.w};
+#pragma unroll
+    for (int k = 0; k < NV; ++k) umin[k] = umax[k] = u0[k];
+  }
 #pragma unroll
   for (int j = 0; j < D; ++j) {
     bo[j] = 0.f;
@@ -787,6 +779,14 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
       const float du = u1[NV - 1] + nu0s[NV - 1];
 #pragma unroll
       for (int j = 0; j < D; ++j) bo[j] += du * dx[j];
+    }
+    {
+      const float u1[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        umin[k] = fminf(u1[k], umin[k]);
+        umax[k] = fmaxf(u1[k], umax[k]);
+      }
     }
   }
   // closed-form solve, g = M^-1 b, per slot pair (go: the odd slot)
@@ -850,32 +850,6 @@ __device__ __forceinline__ void cell_gradients_pairs(const workspace &w, int c0,
         for (int i = 1; i < D; ++i) du += go[i] * dxv[i];
         dpos[NV - 1] = fmaxf(du, dpos[NV - 1]);
         dneg[NV - 1] = fminf(du, dneg[NV - 1]);
-      }
-    }
-    // the neighbour extrema (tasks.h:232-236) only when some variable can be
-    // limited: a second pass over the neighbours (min / max do not depend on
-    // the order, so the values are those of a single pass)
-    float umin[NV], umax[NV];
-    bool need = false;
-    {
-      const float u0[8] = {a0.x, a0.y, a0.z, a0.w, b0.x, b0.y, b0.z, b0.w};
-#pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        umin[k] = umax[k] = u0[k];
-        need = need || dpos[k] > tol || dneg[k] < -tol;
-      }
-    }
-    if (need) {
-      for (int q = 0; q < nn; ++q) {
-        float4 a, b;
-        float yh[3], yl[3];
-        nbr(q, a, b, yh, yl);
-        const float u1[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-          umin[k] = fminf(u1[k], umin[k]);
-          umax[k] = fmaxf(u1[k], umax[k]);
-        }
       }
     }
     float phi[NV];

@@ -44,6 +44,7 @@
 #include "fvh_sf64.cuh"
 
 
+
 namespace fvh {
 namespace plain {
 
@@ -82,11 +83,22 @@ struct arith_opt {
     rare |= r.rare;
     return r.q;
   }
+  // x * 0.5 and x / 2, the same correctly rounded value: exact while the
+  // half is a normal number, so the exponent field drops by one; zeros keep
+  // their bits; tiny, infinite and NaN operands are left to the hardware
+  __device__ __forceinline__ double half(double x) {
+    unsigned lo, hi;
+    sf64::halves(x, lo, hi);
+    const unsigned e = sf64::expo(hi);
+    rare |= (unsigned)((e <= 1u) & !sf64::is_zero(lo, hi)) | (unsigned)(e == 0x7ffu);
+    return e > 1u ? sf64::join(lo, hi - (1u << 20)) : x;
+  }
 };
 // ... and with the FP64 instructions (the evaluation kept when `rare`)
 struct arith_hw {
   __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
   __device__ __forceinline__ double quo(double a, double b) { return __ddiv_rn(a, b); }
+  __device__ __forceinline__ double half(double x) { return __dmul_rn(x, 0.5); }
 };
 
 // IEEE comparisons decided on the integer pipe (an FP64 compare would take an
@@ -164,7 +176,7 @@ struct prim {
 
 template <int D, class A>
 __device__ __forceinline__ double total_energy(A &ar, const prim<D> &u) {
-  return u.e + ar.mul(0.5, dot<D>(ar, u.v, u.v));
+  return u.e + ar.half(dot<D>(ar, u.v, u.v));  // 0.5 * |v|^2
 }
 
 template <int D, class A>
@@ -221,9 +233,9 @@ __device__ __forceinline__ void rusanov(A &ar, const prim<D> &l, const prim<D> &
   const double sr = r.a + absval(dot<D>(ar, r.v, n));
   const double s = smax(sl, sr);
   solution_delta<D>(ar, l, r, du);
-  const double half_s = ar.quo(s, 2);
+  const double half_s = ar.half(s);  // s / 2
 #pragma unroll
-  for (int i = 0; i < D + 2; ++i) f[i] = ar.quo(fl[i] + fr[i], 2) - ar.mul(du[i], half_s);
+  for (int i = 0; i < D + 2; ++i) f[i] = ar.half(fl[i] + fr[i]) - ar.mul(du[i], half_s);
 }
 
 // Toro's HLLC (sec. 10.4) with the hlle_flux wave-speed estimates.
@@ -705,28 +717,41 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
 }
 
 // Blocks of 128 per SM the kernels are compiled for.  2D (1024^2 workload, ms
-// per step): gradients 7 (at most 73 registers) 1.813 against 1.845 with 6
-// and 1.887 with 5; fluxes 6 (80 registers) 1.845 against 1.870 with 5 and
-// 1.845 with 7.  3D (96^3 hex, ms per step): gradients and fluxes 5 blocks
-// (96 registers) 5.68 against 5.92 with 3 and 4 and 5.88 with 4 and 5.
+// per step): fluxes 6 (80 registers) 1.845 against 1.870 with 5 and 1.845
+// with 7; gradients 10 (48 registers, variables in pairs, below) 1.572
+// against 1.582 with 8.  3D (96^3 hex): gradients and fluxes 5 blocks (96
+// registers) 5.68 against 5.92 with 3 and 4 and 5.88 with 4 and 5.
 template <int D>
 constexpr int min_blocks() { return D == 2 ? 6 : 5; }
 template <int D>
-constexpr int grad_min_blocks() { return D == 2 ? 7 : 5; }
-// variables per neighbour pass of the gradients: all of them in 2D; in 3D
-// (7 variables x 3 components) two passes, d v and e p a
+constexpr int grad_min_blocks() { return D == 2 ? 10 : 5; }
+// Variables per neighbour pass of the gradients.  Each variable's gradient
+// and limiter depend on that variable alone, so the variables can be taken in
+// groups, each in its own pass over the neighbours (the neighbours' values
+// are re-read, mostly from L1/L2): fewer live sums, more warps.  2D in pairs
+// (d vx, vy e, p a): 1.572 ms per step against 1.755 with all six in one pass
+// and 1.592 in threes; 3D in groups of four (d v, then e p a): 5.30 against
+// 5.58 in threes (6 blocks) and 5.30 in pairs.
 template <int D>
-__host__ __device__ constexpr int grad_split() { return D == 2 ? D + 4 : D + 1; }
+__host__ __device__ constexpr int grad_split() { return D == 2 ? 2 : D + 1; }
+
+// the variables K0 .. NV-1 in groups of G, each group in its own pass
+template <int D, int K0, int G, bool LIMIT, bool PRE>
+__device__ __forceinline__ void gradient_groups(const fvh_mesh_view &m, const fvh_state_view &s,
+                                                const fvh_gradient_view &g, const tables &t,
+                                                int c0) {
+  constexpr int NV = D + 4, NK = (NV - K0 < G) ? NV - K0 : G;
+  gradient_group<D, K0, NK, LIMIT, PRE>(m, s, g, t, c0);
+  if constexpr (K0 + NK < NV) gradient_groups<D, K0 + NK, G, LIMIT, PRE>(m, s, g, t, c0);
+}
 
 template <int D, bool LIMIT, bool PRE>
 __global__ void __launch_bounds__(kCellThreads, grad_min_blocks<D>())
 gradients_kernel(const fvh_mesh_view m, const fvh_state_view s, const fvh_gradient_view g,
                  const tables t) {
-  constexpr int NV = D + 4, S = grad_split<D>();
   const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (c0 >= m.num_cells) return;
-  gradient_group<D, 0, S, LIMIT, PRE>(m, s, g, t, c0);
-  if constexpr (S < NV) gradient_group<D, S, NV - S, LIMIT, PRE>(m, s, g, t, c0);
+  gradient_groups<D, 0, grad_split<D>(), LIMIT, PRE>(m, s, g, t, c0);
 }
 
 // ---------------------------------------------------------------------------
@@ -905,11 +930,11 @@ __device__ __forceinline__ void cell_update(A &ar, const fvh_mesh_view &m,
   const double den0 = s.density[c];
   const double mass = den0 + du[0];
   const double ener =
-      ar.mul(den0, s.internal_energy[c] + ar.mul(0.5, dot<D>(ar, vel, vel))) + du[D + 1];
+      ar.mul(den0, s.internal_energy[c] + ar.half(dot<D>(ar, vel, vel))) + du[D + 1];
   const double inv_mass = ar.quo(1, mass);
 #pragma unroll
   for (int i = 0; i < D; ++i) vel[i] = ar.mul(ar.mul(den0, vel[i]) + du[1 + i], inv_mass);
-  const double e = ar.mul(ener, inv_mass) - ar.mul(0.5, dot<D>(ar, vel, vel));
+  const double e = ar.mul(ener, inv_mass) - ar.half(dot<D>(ar, vel, vel));
   w[0] = mass;
 #pragma unroll
   for (int i = 0; i < D; ++i) w[1 + i] = vel[i];
