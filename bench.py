@@ -445,6 +445,29 @@ def run_serving(torch, stream, batched_rate: float, seconds: float, seed: int = 
     return rep
 
 
+def roofline_3d(mesh, form: str, prof: dict, in_run_step_ms: float) -> dict:
+    """Dominant kernel of a 3D form against HBM: the reference dataflow's bytes
+    of its task (the plain form's per-cell figures, 412 B/cell for the
+    gradients in 3D), the duration its profiled share of the in-run step."""
+    hbm, peak_kind = peaks()
+    ab = algorithmic_bytes(mesh, "fp64")
+    task = {"gradients": "gradients", "fluxes": "fluxes", "update": "update", "dt": "dt",
+            "face_flux": "fluxes", "gather_update": "update", "pack_dt": "dt"}
+    profiled = sum(v[0] * v[1] for v in prof.values())
+    scale = in_run_step_ms / profiled
+    dom = max(prof, key=lambda k: prof[k][0] * prof[k][1])
+    dur = prof[dom][0] * scale
+    sb = ab[task[dom]]
+    return {"bound": "hbm", "kernel": dom, "duration_ms": dur,
+            "algorithmic_bytes_per_launch": sb,
+            "bytes_basis": f"reference-dataflow bytes of the {task[dom]} task "
+                           f"({sb / mesh.num_cells:.0f} B/cell)",
+            "achieved": sb / (dur * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": sb / (dur * 1e-3) / 1e9 / hbm, "peak_source": peak_kind,
+            "kernels": {k: {"duration_ms": v[0] * scale, "launches_per_step": v[1],
+                            "share": v[0] * v[1] / profiled} for k, v in prof.items()}}
+
+
 def run_3d(torch, stream, n: int = 192, steps: int = 100, shape: str = "") -> dict:
     """192^3 hex shock box (inner cube [0,0.5]^3 at rho=1,p=1, rest 0.125/0.1),
     jitter +-0.15h (seed 2), Rusanov, CFL 0.3, 100 steps: FP64 vs mixed.  The
@@ -484,7 +507,8 @@ def run_3d(torch, stream, n: int = 192, steps: int = 100, shape: str = "") -> di
             raise RuntimeError(f"3d {form}: status {code}")
         res[form] = ds.download(stream)
         out[form] = {"value": mesh.num_cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-                     "t_final": t}
+                     "t_final": t, "roofline": roofline_3d(mesh, form, sv.profile(ds, 4, stream),
+                                                           ms / steps)}
         del sv, ds
     f, m = res["fp64"], res["mixed"]
     E = lambda s: s[0] * (s[4] + 0.5 * (s[1] ** 2 + s[2] ** 2 + s[3] ** 2))

@@ -472,7 +472,7 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
 
 fvh_status fvh_debug_sf64(int32_t op, const double *a, const double *b, int64_t n,
                           double *out, fvh_stream_t stream) {
-  if (op < 0 || op > 9 || n < 0 || (n > 0 && (!a || !b || !out)))
+  if (op < 0 || op > 10 || n < 0 || (n > 0 && (!a || !b || !out)))
     return FVH_ERR_INVALID_ARGUMENT;
   return from_cuda(fvh::plain::debug_sf64(op, a, b, n, out, cs(stream)));
 }

@@ -1044,6 +1044,12 @@ __global__ void sf64_kernel(int op, const double *a, const double *b, int64_t n,
         r = sf64::mul_opt(x, y, rare);
         if (rare) r = __dmul_rn(x, y);
         break;
+      case 10: {  // the kernels' halving of x (0.5 * x and x / 2), with its redo
+        arith_opt ar;
+        r = ar.half(x);
+        if (ar.rare) r = __dmul_rn(x, 0.5);
+        break;
+      }
       default:
         r = sf64::div_opt(x, y, rare);
         if (rare) r = __ddiv_rn(x, y);

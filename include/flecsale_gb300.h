@@ -317,8 +317,10 @@ fvh_status fvh_debug_split(const double *x, int64_t n, float *hi, float *lo, flo
  * 3 = divide, each correctly rounded to nearest-even on the integer/FP32
  * pipes; op 4..7 = the same four with the FP64 instructions; op 8 / 9 = the
  * FP64 kernels' branch-free multiply / divide, redone with the FP64
- * instruction where they flag an operand.  All must agree bit for bit with
- * the FP64 instructions on every input.  No reference counterpart. */
+ * instruction where they flag an operand; op 10 = the kernels' halving of
+ * a[i] (0.5 * a and a / 2; b unused), redone likewise.  All must agree bit
+ * for bit with the FP64 instructions on every input.  No reference
+ * counterpart. */
 fvh_status fvh_debug_sf64(int32_t op, const double *a, const double *b, int64_t n,
                           double *out, fvh_stream_t stream);
 

@@ -6,8 +6,8 @@ instructions (ops 4..7 of the same entry point) and as the host's IEEE
 arithmetic (numpy), for every input: operand classes that take the integer
 path (normal operands and results, zeros) and those that go to the hardware
 (subnormals, infinities, NaNs, overflow and underflow).  The optimistic
-multiply and divide the kernels use (ops 8 and 9, with their FP64 redo) are
-held to the same bar.  NaN results are compared as NaN, whatever their
+multiply and divide the kernels use (ops 8 and 9, with their FP64 redo) and
+their halving of a value (op 10) are held to the same bar.  NaN results are compared as NaN, whatever their
 payload.
 """
 import numpy as np
@@ -106,3 +106,13 @@ def test_integer_pipe_arithmetic_is_ieee(cuda, mode):
         assert not bad.any(), (pair, a[bad][:4], b[bad][:4], got[0][bad][:4], got[1][bad][:4])
         bad = ~_same(got[0], host[op])
         assert not bad.any(), (pair, a[bad][:4], b[bad][:4], got[0][bad][:4], host[op][bad][:4])
+    # op 10: the kernels' exact halving (0.5 * a and a / 2 are one value)
+    # against the host's 0.5 * a, on every operand class (tiny halves round)
+    H.check(L.fvh_debug_sf64(10, da.data_ptr(), db.data_ptr(), N, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    with np.errstate(all="ignore"):
+        want = a * 0.5
+        assert np.array_equal(want, a / 2, equal_nan=True)
+    bad = ~_same(got, want)
+    assert not bad.any(), (a[bad][:4], got[bad][:4], want[bad][:4])
