@@ -410,6 +410,11 @@ def run_batched(torch, stream, steps: int, warmup: int) -> dict:
             "launches": "one CUDA graph launch for all steps",
             "gpu_launches": b.launches_per_step() * steps + 1,  # + the first step's pack
             "autotuned_shape": tune, "host_setup_s": setup_s,
+            "tuned_space": "block 128/256 x cells per thread 1/2 x gather schedule 0 (cell-centric "
+                           "fluxes) / 1 (face-flux array); the face-colouring schedule is not a "
+                           "batch candidate: its per-colour launches scatter over the whole "
+                           "concatenated mesh (2.6x slower than gather on one 1024^2 mesh) and "
+                           "a batch reassignment would have to recolour it on the host",
             "accuracy_vs_fp64": acc,
             "config": "512 independent 2D problems, cells log-uniform in [32^2, 512^2] (seed 3), "
                       "KH shear layer / four-quadrant / Sod, HLLC, outflow, textbook reconstruction, CFL 0.4, "
