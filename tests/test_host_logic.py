@@ -59,6 +59,24 @@ def test_algorithmic_bytes_model():
     assert bench.per_zone_update_bytes(m3, "fp64") > f  # 3D moves more per zone-update
 
 
+def test_roofline_3d_from_a_profile():
+    """The 3D roofline: the dominant kernel by time share, its duration scaled
+    to the in-run step, the gradients task's reference-dataflow bytes (about
+    412 B/cell for hexes with 26 neighbours) over that duration."""
+    import bench
+    m3 = H.HostMesh.box(3, (8, 8, 8), [0, 0, 0], [1, 1, 1], 0.1, 1)
+    prof = {"pack_dt": (0.2, 0.25), "gradients": (1.0, 2.0), "face_flux": (0.5, 2.0),
+            "gather_update": (0.4, 2.0)}
+    r = bench.roofline_3d(m3, "mixed", prof, in_run_step_ms=(0.05 + 2.0 + 1.0 + 0.8) / 2)
+    assert r["kernel"] == "gradients"
+    assert abs(r["duration_ms"] - 0.5) < 1e-12      # profiled 1.0 ms, step scaled by 1/2
+    sb = bench.algorithmic_bytes(m3, "fp64")["gradients"]
+    assert r["algorithmic_bytes_per_launch"] == sb
+    assert abs(r["achieved"] - sb / 0.5e-3 / 1e9) < 1e-9
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    assert abs(sum(k["share"] for k in r["kernels"].values()) - 1.0) < 1e-12
+
+
 def test_max_over_ranks_without_a_group():
     import bench
     assert bench.max_over_ranks(None, 3.5) == 3.5
