@@ -17,12 +17,14 @@
 // lexicographic numbering the neighbours of a warp's cells share cache lines and
 // are served from L1/L2 after the first touch.
 //
-// Pipes: GB300 issues 2 FP64 operations per clock per SM.  Every product and
-// quotient below is computed on the integer/FP32 pipes by the correctly
-// rounded routines of fvh_sf64.cuh, while sums and differences stay on the
-// FP64 pipe; comparisons, minima and maxima run on integer order keys.  Both
-// pipes round to nearest-even exactly as IEEE binary64 does, so the bits are
-// unchanged, and they work at the same time.  Each unit of work (a cell or a
+// Pipes: GB300 issues 2 FP64 operations per clock per SM.  Most products and
+// every quotient below are computed on the integer/FP32 pipes by the
+// correctly rounded routines of fvh_sf64.cuh, while most sums and differences
+// stay on the FP64 pipe; each kernel moves a part of one kind to the other
+// pipe so that both are loaded alike (fp64_products, add_call).  Comparisons,
+// minima and maxima run on integer order keys.  Both pipes round to
+// nearest-even exactly as IEEE binary64 does, so the bits are unchanged, and
+// they work at the same time.  Each unit of work (a cell or a
 // face) is evaluated optimistically with the branch-free integer forms
 // (arith_opt); if any operand was of a kind they do not handle (subnormal,
 // infinite, NaN, beyond 2^+-500) the unit is evaluated again with the FP64
@@ -34,7 +36,8 @@
 // loops rolled, evaluate each physical flux once per side (selecting the
 // state instead of branching into copies), and take products, quotients and
 // the FP64 redo of a rare unit in out-of-line calls (2.27 -> 1.77 ms per 2D
-// step on the 1024^2 workload).
+// step on the 1024^2 workload; the pipe balance and the variable groups of
+// the gradients below took it on to 1.49 ms).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -42,8 +45,6 @@
 #include "flecsale_gb300.h"
 #include "fvh_kernels.h"
 #include "fvh_sf64.cuh"
-
-
 
 namespace fvh {
 namespace plain {
@@ -62,15 +63,15 @@ __device__ __noinline__ flagged mul_call(double a, double b) {
   r.q = sf64::mul_opt(a, b, r.rare);
   return r;
 }
-// A sum on the integer pipe (correctly rounded; rare operands inside go to the
-// hardware instruction), for a kernel whose FP64 pipe is the busier one.
-__device__ __noinline__ double add_call(double a, double b) { return sf64::add(a, b); }
 __device__ __noinline__ flagged div_call(double a, double b) {
   flagged r;
   r.rare = 0;
   r.q = sf64::div_opt(a, b, r.rare);
   return r;
 }
+// A sum on the integer pipe (correctly rounded; rare operands inside go to the
+// hardware instruction), for a kernel whose FP64 pipe is the busier one.
+__device__ __noinline__ double add_call(double a, double b) { return sf64::add(a, b); }
 
 // Products and quotients of one unit of work: on the integer pipes, noting
 // any operand they leave to the hardware ...
@@ -743,14 +744,18 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
 }
 
 // Blocks of 128 per SM the kernels are compiled for.  2D (1024^2 workload, ms
-// per step): fluxes 6 (80 registers) 1.845 against 1.870 with 5 and 1.845
-// with 7; gradients 10 (48 registers, variables in pairs, below) 1.572
-// against 1.582 with 8.  3D (96^3 hex): gradients and fluxes 5 blocks (96
-// registers) 5.68 against 5.92 with 3 and 4 and 5.88 with 4 and 5.
+// per step): fluxes 7 (72 registers) 1.493 against 1.502 with 6 and 1.542
+// with 8; gradients 10 (48 registers, variables in pairs, below) 1.572
+// against 1.582 with 8; update 10 (48 registers) 1.487 against 1.502 with
+// the compiler's choice (66 registers) and 1.493 with 8.  3D (96^3 hex):
+// gradients and fluxes 5 blocks (96 registers) 5.68 against 5.92 with 3 and
+// 4 and 5.88 with 4 and 5; update the compiler's choice.
 template <int D>
-constexpr int min_blocks() { return D == 2 ? 6 : 5; }
+constexpr int min_blocks() { return D == 2 ? 7 : 5; }
 template <int D>
 constexpr int grad_min_blocks() { return D == 2 ? 10 : 5; }
+template <int D>
+constexpr int update_min_blocks() { return D == 2 ? 10 : 1; }
 // Variables per neighbour pass of the gradients.  Each variable's gradient
 // and limiter depend on that variable alone, so the variables can be taken in
 // groups, each in its own pass over the neighbours (the neighbours' values
@@ -984,7 +989,7 @@ __device__ __forceinline__ void cell_update(A &ar, const fvh_mesh_view &m,
 }
 
 template <int D>
-__global__ void __launch_bounds__(kCellThreads)
+__global__ void __launch_bounds__(kCellThreads, update_min_blocks<D>())
 update_kernel(const fvh_mesh_view m, const fvh_flux_view fl, const fvh_state_view s,
               const double *dt, double factor, double gm1, double ggm1, double cv,
               double *soln_time, fvh_device_status *status, const fvh_state_view out,
