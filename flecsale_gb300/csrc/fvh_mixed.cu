@@ -945,12 +945,12 @@ gradients_kernel(const fvh_mesh_view m, workspace w, const float4 *__restrict__ 
 // a mesh numbered row by row these sets are a few runs of consecutive ids.  The
 // setup lists each chunk's runs and packs, per cell, its own record's position
 // and those of its neighbours and vertices in the chunk's staged set (a byte
-// each, four to a 32-bit word).  A persistent kernel posts the copies of chunk
-// i+1 (one bulk copy per
-// run and array, plus one for the chunk's topology; completion counted on an
-// mbarrier) while its threads compute chunk i from shared memory with the
-// arithmetic of gradients_kernel (cell_gradients_pairs), so both kernels give
-// the same bits.
+// each, four to a 32-bit word), and sizes the stage buffers for the mesh's
+// largest chunk.  A persistent kernel posts the copies of chunk i+1 (one bulk
+// copy per run and array, plus one for the chunk's topology; completion
+// counted on an mbarrier) while its threads compute chunk i from shared memory
+// with the arithmetic of gradients_kernel (cell_gradients_pairs), so both
+// kernels give the same bits.
 constexpr int kStageCells = 128;      // cells per chunk = threads per block
 constexpr int kStageMaxCells = 256;   // staged cell records per chunk (byte slots)
 constexpr int kStageMaxVerts = 256;   // staged vertex records per chunk
