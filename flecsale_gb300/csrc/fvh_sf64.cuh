@@ -264,14 +264,17 @@ __device__ __forceinline__ double mul_opt(double a, double b, unsigned &rare) {
   unsigned al, ah, bl, bh;
   halves(a, al, ah);
   halves(b, bl, bh);
-  const unsigned ea = expo(ah), eb = expo(bh);
+  // A zero times a finite value is a zero; (a zero) & finite(b) | (b zero) &
+  // finite(a) is (either zero) & finite(a) & finite(b).  Fewer instructions
+  // than testing each case apart (2D FP64 step 1.474 -> 1.451 ms).
+  const unsigned ha = ah & 0x7fffffffu, hb = bh & 0x7fffffffu;
+  const unsigned ea = ha >> 20, eb = hb >> 20;
   const unsigned sign = (ah ^ bh) & 0x80000000u;
-  const bool za = is_zero(al, ah), zb = is_zero(bl, bh);
+  const bool zero = ((ha | al) == 0u) | ((hb | bl) == 0u);
   const bool fast = moderate(ea) & moderate(eb);
-  const bool zero = (za & is_finite(bh)) | (zb & is_finite(ah));
-  rare |= (unsigned)!(fast | zero);
+  rare |= (unsigned)!(fast | (zero & (ea != 0x7ffu) & (eb != 0x7ffu)));
   const double q = mul_core(al, ah, bl, bh, ea, eb, sign);
-  return (za | zb) ? join(0u, sign) : q;
+  return zero ? join(0u, sign) : q;
 }
 
 __device__ __forceinline__ double div_opt(double a, double b, unsigned &rare) {
