@@ -704,28 +704,28 @@ __device__ __forceinline__ void cell_gradients(A &ar, const fvh_mesh_view &m,
   }
 }
 
-// the gradients of variables K0 .. K0+NK-1 of cell c0, stored
-template <int D, int K0, int NK, bool LIMIT, bool PRE, class A>
-__device__ __forceinline__ void gradient_group_with(A &ar, const fvh_mesh_view &m,
-                                                    const fvh_state_view &s,
-                                                    const fvh_gradient_view &g, const tables &t,
-                                                    int c0) {
-  double gu[NK][D];
-  cell_gradients<D, K0, NK, LIMIT, PRE>(ar, m, s, t, c0, gu);
+template <int D, int K0, int NK>
+__device__ __forceinline__ void store_gradients(const fvh_gradient_view &g, int c0,
+                                                const double (&gu)[NK][D]) {
 #pragma unroll
   for (int k = 0; k < NK; ++k)
 #pragma unroll
     for (int i = 0; i < D; ++i) grad_plane<D>(g, K0 + k, i)[c0] = gu[k][i];
 }
 
+// the FP64 redo of a cell whose operands left the integer-pipe range, out of
+// line (it is rare and would otherwise double the kernel's code)
 template <int D, int K0, int NK, bool LIMIT, bool PRE>
 __device__ __noinline__ void gradient_group_hw(const fvh_mesh_view &m, const fvh_state_view &s,
                                                const fvh_gradient_view &g, const tables &t,
                                                int c0) {
+  double gu[NK][D];
   arith_hw hw;
-  gradient_group_with<D, K0, NK, LIMIT, PRE>(hw, m, s, g, t, c0);
+  cell_gradients<D, K0, NK, LIMIT, PRE>(hw, m, s, t, c0, gu);
+  store_gradients<D, K0, NK>(g, c0, gu);
 }
 
+// the gradients of variables K0 .. K0+NK-1 of cell c0, stored
 template <int D, int K0, int NK, bool LIMIT, bool PRE>
 __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh_state_view &s,
                                                const fvh_gradient_view &g, const tables &t,
@@ -737,10 +737,7 @@ __device__ __forceinline__ void gradient_group(const fvh_mesh_view &m, const fvh
     gradient_group_hw<D, K0, NK, LIMIT, PRE>(m, s, g, t, c0);
     return;
   }
-#pragma unroll
-  for (int k = 0; k < NK; ++k)
-#pragma unroll
-    for (int i = 0; i < D; ++i) grad_plane<D>(g, K0 + k, i)[c0] = gu[k][i];
+  store_gradients<D, K0, NK>(g, c0, gu);
 }
 
 // Blocks of 128 per SM the kernels are compiled for.  2D (1024^2 workload, ms
@@ -885,6 +882,8 @@ __device__ __forceinline__ void face_flux(A &ar, const fvh_mesh_view &m,
   for (int k = 0; k < D + 2; ++k) F[k] = __dmul_rn(F[k], area);
 }
 
+// the FP64 redo of a face whose operands left the integer-pipe range, out of
+// line
 template <int D, int KIND, bool SECOND, bool PRE>
 __device__ __noinline__ void face_flux_hw(const fvh_mesh_view &m, const fvh_state_view &s,
                                           const fvh_gradient_view &g, const fvh_flux_view &fl,
